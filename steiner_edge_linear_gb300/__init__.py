@@ -1,0 +1,453 @@
+"""GB300-native Erickson-Monma-Veinott Steiner solver.
+
+Python face of the C ABI in ``include/emv.h`` (loaded with ctypes from the
+in-tree ``lib/libemv.so``).  The names mirror the reference solver's own
+functions in reader/reader-el.c:
+
+  ``graph_load(path)``              -> graph_load          (R:473-618)
+  ``root_build(g)``                 -> root_build          (R:706-899)
+  ``erickson_monma_veinott(r, l)``  -> erickson_monma_veinott (R:2141-2343)
+  ``Solver.kernel_dev(...)``        -> emv_kernel          (R:1966-2139)
+  ``Solver.sssp(...)``              -> dijkstra            (R:1762-1880)
+
+There is no CPU fallback: every solve runs the sm_103a kernels, and loading
+fails loudly when the library has not been built.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass, field
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import build as _build
+
+INF32 = 1 << 30
+LIB_PATH = _build.LIB_PATH
+CLI_PATH = _build.CLI_PATH
+
+TREE = 0x1
+TABLE = 0x2
+NOCHECK = 0x4
+
+STATUS = {
+    0: "EMV_OK", 1: "EMV_ERR_BAD_INPUT", 2: "EMV_ERR_PARSE", 3: "EMV_ERR_OOM", 4: "EMV_ERR_OVER_BUDGET",
+    5: "EMV_ERR_TIMEOUT", 6: "EMV_ERR_CUDA", 7: "EMV_ERR_DISCONNECTED", 8: "EMV_ERR_OVERFLOW",
+    9: "EMV_ERR_NOT_READY", 10: "EMV_ERR_CANCELLED", 11: "EMV_ERR_INTERNAL",
+}
+ERR_NOT_READY = 9
+
+
+class EmvError(RuntimeError):
+    """A non-zero emv status, with the library's message."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+# ----------------------------------------------------------------- C structs
+
+class _Stp(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64), ("m", ctypes.c_int64), ("k", ctypes.c_int64), ("cost", ctypes.c_int64),
+                ("edges", ctypes.POINTER(ctypes.c_int64)), ("terminals", ctypes.POINTER(ctypes.c_int64))]
+
+
+class _Graph(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int32), ("arcs", ctypes.c_int64), ("row_ptr", ctypes.c_void_p),
+                ("col", ctypes.c_void_p), ("w", ctypes.c_void_p)]
+
+
+class _Timing(ctypes.Structure):
+    _fields_ = [("zero_ms", ctypes.c_float), ("level1_ms", ctypes.c_float), ("merge_ms", ctypes.c_float),
+                ("relax_ms", ctypes.c_float), ("traceback_ms", ctypes.c_float), ("kernel_ms", ctypes.c_float),
+                ("relax_sweeps", ctypes.c_int64), ("launches", ctypes.c_int64)]
+
+
+class _Result(ctypes.Structure):
+    _fields_ = [("cost", ctypes.c_int64), ("tree", ctypes.c_void_p), ("tree_cap", ctypes.c_int64),
+                ("tree_count", ctypes.c_int64), ("tree_weight", ctypes.c_int64), ("table", ctypes.c_void_p),
+                ("timing", _Timing)]
+
+
+class _Instance(ctypes.Structure):
+    _fields_ = [("g", _Graph), ("terminals", ctypes.c_void_p), ("k", ctypes.c_int32)]
+
+
+class _BatchStats(ctypes.Structure):
+    _fields_ = [("total_ms", ctypes.c_float), ("upload_ms", ctypes.c_float), ("work_items", ctypes.c_int64),
+                ("table_bytes", ctypes.c_int64), ("merge_tile", ctypes.c_int32), ("relax_rows", ctypes.c_int32)]
+
+
+class _ServerOpts(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_int64), ("max_slots", ctypes.c_int32),
+                ("large_n", ctypes.c_int32)]
+
+
+class _ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_int64), ("completed", ctypes.c_int64), ("rejected", ctypes.c_int64),
+                ("waves", ctypes.c_int64), ("peak_resident", ctypes.c_int64), ("peak_bytes", ctypes.c_int64)]
+
+
+_P = ctypes.c_void_p
+_I32 = ctypes.c_int32
+_I64 = ctypes.c_int64
+_U64 = ctypes.c_uint64
+
+# name -> (restype, argtypes); the list of exported entry points of include/emv.h
+SIGNATURES = {
+    "emv_status_str": (ctypes.c_char_p, [ctypes.c_int]),
+    "emv_last_error": (ctypes.c_char_p, []),
+    "emv_version": (ctypes.c_char_p, []),
+    "emv_stp_parse": (ctypes.c_int, [ctypes.c_char_p, _I64, ctypes.POINTER(ctypes.POINTER(_Stp))]),
+    "emv_stp_load": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.POINTER(_Stp))]),
+    "emv_stp_free": (None, [ctypes.POINTER(_Stp)]),
+    "emv_stp_write": (ctypes.c_int, [ctypes.POINTER(_Stp), ctypes.c_char_p]),
+    "emv_csr_build": (ctypes.c_int, [_I64, _I64, _P, _P, _P, _P]),
+    "emv_graph_check": (ctypes.c_int, [ctypes.POINTER(_Graph), ctypes.POINTER(_I64)]),
+    "emv_gen_regular": (ctypes.c_int, [_I64, _I32, _I32, _I32, _I32, _U64, ctypes.POINTER(ctypes.POINTER(_Stp))]),
+    "emv_gen_mixed": (ctypes.c_int, [_U64, _I64, _I32, _I32, _I32, _I32, _I32,
+                                     ctypes.POINTER(ctypes.POINTER(_Stp))]),
+    "emv_create": (ctypes.c_int, [ctypes.POINTER(_P), _I32]),
+    "emv_destroy": (ctypes.c_int, [_P]),
+    "emv_kernel_dev": (ctypes.c_int, [_P, _I32, _I64, _P, _P, _P, _I32, _P, _P, _I64, ctypes.POINTER(_I64), _P]),
+    "emv_solve": (ctypes.c_int, [_P, ctypes.POINTER(_Graph), _P, _I32, _I32, ctypes.POINTER(_Result), _P]),
+    "emv_solve_dev": (ctypes.c_int, [_P, ctypes.POINTER(_Graph), _P, _I32, _I32, ctypes.POINTER(_Result), _P]),
+    "emv_sssp": (ctypes.c_int, [_P, ctypes.POINTER(_Graph), _I32, _P, ctypes.POINTER(ctypes.c_float), _P]),
+    "emv_batch_solve": (ctypes.c_int, [_P, ctypes.POINTER(_Instance), _I32, _P, ctypes.POINTER(_BatchStats), _P]),
+    "emv_server_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.POINTER(_ServerOpts)]),
+    "emv_server_submit": (ctypes.c_int, [_P, ctypes.POINTER(_Graph), _P, _I32, ctypes.POINTER(_I64)]),
+    "emv_server_poll": (ctypes.c_int, [_P, _I64, ctypes.POINTER(_I64), ctypes.POINTER(ctypes.c_double)]),
+    "emv_server_wait": (ctypes.c_int, [_P, _I64, ctypes.POINTER(_I64), ctypes.POINTER(ctypes.c_double),
+                                       ctypes.c_double]),
+    "emv_server_cancel": (ctypes.c_int, [_P, _I64]),
+    "emv_server_stats_get": (ctypes.c_int, [_P, ctypes.POINTER(_ServerStats)]),
+    "emv_server_destroy": (ctypes.c_int, [_P]),
+}
+
+_lib: Optional[ctypes.CDLL] = None
+
+
+def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
+    """Loads libemv.so once and declares every entry point; raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build the CUDA library first "
+                           "(python -c 'import __graft_entry__ as g; g.build()')")
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name, None)
+        if fn is None:
+            continue
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _check(status: int) -> None:
+    if status != 0:
+        msg = load_library().emv_last_error().decode(errors="replace")
+        raise EmvError(status, msg)
+
+
+def _ptr(a: Optional[np.ndarray]) -> Optional[int]:
+    return None if a is None else a.ctypes.data
+
+
+# ------------------------------------------------------------------ instances
+
+@dataclass
+class StpInstance:
+    """A parsed or generated instance (the reference's graph_t, R:358-373)."""
+
+    n: int
+    edges: np.ndarray      # (m, 3) int64: u, v, w, 0-based
+    terminals: np.ndarray  # (k,) int64, 0-based
+    cost: int = -1
+
+    @property
+    def m(self) -> int:
+        return int(self.edges.shape[0])
+
+    @property
+    def k(self) -> int:
+        return int(self.terminals.shape[0])
+
+    @staticmethod
+    def _take(p) -> "StpInstance":
+        lib = load_library()
+        s = p.contents
+        edges = np.ctypeslib.as_array(s.edges, shape=(int(s.m) * 3,)).reshape(-1, 3).copy() if s.m else \
+            np.zeros((0, 3), np.int64)
+        terms = np.ctypeslib.as_array(s.terminals, shape=(int(s.k),)).copy() if s.k else np.zeros(0, np.int64)
+        out = StpInstance(int(s.n), edges, terms, int(s.cost))
+        lib.emv_stp_free(p)
+        return out
+
+    @staticmethod
+    def from_file(path: str) -> "StpInstance":
+        p = ctypes.POINTER(_Stp)()
+        _check(load_library().emv_stp_load(path.encode(), ctypes.byref(p)))
+        return StpInstance._take(p)
+
+    @staticmethod
+    def from_text(text: str | bytes) -> "StpInstance":
+        b = text.encode() if isinstance(text, str) else text
+        p = ctypes.POINTER(_Stp)()
+        _check(load_library().emv_stp_parse(b, len(b), ctypes.byref(p)))
+        return StpInstance._take(p)
+
+    @staticmethod
+    def regular(n: int, degree: int, wmin: int, wmax: int, k: int, seed: int) -> "StpInstance":
+        """Random d-regular instance (configuration model, connected; emv_gen_regular)."""
+        p = ctypes.POINTER(_Stp)()
+        _check(load_library().emv_gen_regular(n, degree, wmin, wmax, k, seed, ctypes.byref(p)))
+        return StpInstance._take(p)
+
+    @staticmethod
+    def mixed(base_seed: int, index: int, nmin: int = 64, nmax: int = 4096, kmin: int = 4, kmax: int = 10,
+              group_pct: int = 10) -> "StpInstance":
+        """Instance ``index`` of the mixed batched distribution (emv_gen_mixed)."""
+        p = ctypes.POINTER(_Stp)()
+        _check(load_library().emv_gen_mixed(base_seed, index, nmin, nmax, kmin, kmax, group_pct, ctypes.byref(p)))
+        return StpInstance._take(p)
+
+    def write(self, path: str) -> None:
+        e = np.ascontiguousarray(self.edges, dtype=np.int64).reshape(-1)
+        t = np.ascontiguousarray(self.terminals, dtype=np.int64)
+        s = _Stp(self.n, self.m, self.k, self.cost, e.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                 t.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+        _check(load_library().emv_stp_write(ctypes.byref(s), path.encode()))
+
+
+@dataclass
+class Csr:
+    """Host int32 CSR with both arcs of every edge (root_build, R:706-899)."""
+
+    n: int
+    row_ptr: np.ndarray
+    col: np.ndarray
+    w: np.ndarray
+    terminals: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    cost: int = -1
+
+    @property
+    def arcs(self) -> int:
+        return int(self.col.shape[0])
+
+    @property
+    def k(self) -> int:
+        return int(self.terminals.shape[0])
+
+    @staticmethod
+    def from_stp(g: StpInstance) -> "Csr":
+        n, m = g.n, g.m
+        row = np.zeros(n + 1, np.int32)
+        col = np.zeros(max(2 * m, 1), np.int32)
+        w = np.zeros(max(2 * m, 1), np.int32)
+        e = np.ascontiguousarray(g.edges, dtype=np.int64).reshape(-1)
+        _check(load_library().emv_csr_build(n, m, _ptr(e), _ptr(row), _ptr(col), _ptr(w)))
+        return Csr(n, row, col[:2 * m], w[:2 * m], np.ascontiguousarray(g.terminals, dtype=np.int32), g.cost)
+
+    def c_graph(self) -> _Graph:
+        return _Graph(self.n, self.arcs, _ptr(self.row_ptr), _ptr(self.col), _ptr(self.w))
+
+    def check(self) -> int:
+        """Connectivity and int32-range check (emv_graph_check); returns the value bound."""
+        b = ctypes.c_int64()
+        g = self.c_graph()
+        _check(load_library().emv_graph_check(ctypes.byref(g), ctypes.byref(b)))
+        return int(b.value)
+
+
+@dataclass
+class Result:
+    cost: int
+    tree: Optional[np.ndarray]      # (count, 3) int32: u, v, w
+    tree_weight: int
+    table: Optional[np.ndarray]     # (2^k, n) int32
+    timing: dict
+
+
+def _timing(t: _Timing) -> dict:
+    return {f: getattr(t, f) for f, _ in _Timing._fields_}
+
+
+class Solver:
+    """A solver context on one CUDA device (emv_create / emv_destroy)."""
+
+    def __init__(self, device: int = 0):
+        self._lib = load_library()
+        self._ctx = ctypes.c_void_p()
+        _check(self._lib.emv_create(ctypes.byref(self._ctx), device))
+
+    def close(self) -> None:
+        if self._ctx:
+            self._lib.emv_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p()
+
+    def __enter__(self) -> "Solver":
+        return self
+
+    def __exit__(self, *exc) -> None:
+        self.close()
+
+    def __del__(self) -> None:
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def solve(self, g: Csr, terminals: Optional[Sequence[int]] = None, tree: bool = False, table: bool = False,
+              check: bool = True, stream: Optional[int] = None) -> Result:
+        """erickson_monma_veinott on a host CSR (emv_solve)."""
+        terms = np.ascontiguousarray(g.terminals if terminals is None else terminals, dtype=np.int32)
+        k = int(terms.shape[0])
+        res = _Result()
+        tree_buf = np.zeros((g.n + 1, 3), np.int32) if tree else None
+        tab = np.zeros(((1 << k), g.n), np.int32) if table and k <= 24 else None
+        if tree_buf is not None:
+            res.tree = tree_buf.ctypes.data
+            res.tree_cap = g.n + 1
+        if tab is not None:
+            res.table = tab.ctypes.data
+        flags = (TREE if tree else 0) | (TABLE if table else 0) | (0 if check else NOCHECK)
+        cg = g.c_graph()
+        _check(self._lib.emv_solve(self._ctx, ctypes.byref(cg), terms.ctypes.data, k, flags, ctypes.byref(res),
+                                   stream))
+        tr = tree_buf[:res.tree_count].copy() if tree_buf is not None else None
+        return Result(int(res.cost), tr, int(res.tree_weight), tab, _timing(res.timing))
+
+    def solve_dev(self, n: int, arcs: int, row_ptr: int, col: int, w: int, terminals: Sequence[int],
+                  tree: bool = False, stream: Optional[int] = None) -> Result:
+        """emv_solve_dev on device pointers (e.g. torch tensors' data_ptr())."""
+        terms = np.ascontiguousarray(terminals, dtype=np.int32)
+        res = _Result()
+        tree_buf = np.zeros((n + 1, 3), np.int32) if tree else None
+        if tree_buf is not None:
+            res.tree = tree_buf.ctypes.data
+            res.tree_cap = n + 1
+        cg = _Graph(n, arcs, row_ptr, col, w)
+        _check(self._lib.emv_solve_dev(self._ctx, ctypes.byref(cg), terms.ctypes.data, int(terms.shape[0]),
+                                       TREE if tree else 0, ctypes.byref(res), stream))
+        tr = tree_buf[:res.tree_count].copy() if tree_buf is not None else None
+        return Result(int(res.cost), tr, int(res.tree_weight), None, _timing(res.timing))
+
+    def kernel_dev(self, n: int, arcs: int, row_ptr: int, col: int, w: int, terminals: Sequence[int],
+                   table: int, ld: int, stream: Optional[int] = None) -> int:
+        """emv_kernel on device data and a caller-owned device table (emv_kernel_dev)."""
+        terms = np.ascontiguousarray(terminals, dtype=np.int32)
+        cost = ctypes.c_int64()
+        _check(self._lib.emv_kernel_dev(self._ctx, n, arcs, row_ptr, col, w, int(terms.shape[0]),
+                                        terms.ctypes.data, table, ld, ctypes.byref(cost), stream))
+        return int(cost.value)
+
+    def sssp(self, g: Csr, source: int, stream: Optional[int] = None) -> tuple[np.ndarray, float]:
+        """Single-source distances (the -dijkstra command); INT64_MAX = unreachable."""
+        dist = np.zeros(g.n, np.int64)
+        ms = ctypes.c_float()
+        cg = g.c_graph()
+        _check(self._lib.emv_sssp(self._ctx, ctypes.byref(cg), source, dist.ctypes.data, ctypes.byref(ms), stream))
+        return dist, float(ms.value)
+
+    def batch_solve(self, graphs: Sequence[Csr], stream: Optional[int] = None) -> tuple[np.ndarray, dict]:
+        """Many independent instances in one persistent launch per level (emv_batch_solve)."""
+        count = len(graphs)
+        insts = (_Instance * count)()
+        for i, g in enumerate(graphs):
+            insts[i].g = g.c_graph()
+            insts[i].terminals = g.terminals.ctypes.data
+            insts[i].k = g.k
+        costs = np.zeros(count, np.int64)
+        st = _BatchStats()
+        _check(self._lib.emv_batch_solve(self._ctx, insts, count, costs.ctypes.data, ctypes.byref(st), stream))
+        return costs, {f: getattr(st, f) for f, _ in _BatchStats._fields_}
+
+
+class Server:
+    """Continuous-batching request loop on one GPU (emv_server_*)."""
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 150 * 10**9, max_slots: int = 4096,
+                 large_n: int = 65536):
+        self._lib = load_library()
+        self._srv = ctypes.c_void_p()
+        opts = _ServerOpts(device, hbm_budget_bytes, max_slots, large_n)
+        _check(self._lib.emv_server_create(ctypes.byref(self._srv), ctypes.byref(opts)))
+        self._keep: dict[int, Csr] = {}
+
+    def submit(self, g: Csr) -> int:
+        rid = ctypes.c_int64()
+        cg = g.c_graph()
+        _check(self._lib.emv_server_submit(self._srv, ctypes.byref(cg), g.terminals.ctypes.data, g.k,
+                                           ctypes.byref(rid)))
+        return int(rid.value)
+
+    def poll(self, rid: int) -> Optional[tuple[int, float]]:
+        cost = ctypes.c_int64()
+        lat = ctypes.c_double()
+        st = self._lib.emv_server_poll(self._srv, rid, ctypes.byref(cost), ctypes.byref(lat))
+        if st == ERR_NOT_READY:
+            return None
+        _check(st)
+        return int(cost.value), float(lat.value)
+
+    def wait(self, rid: int, timeout_s: float = 600.0) -> tuple[int, float]:
+        cost = ctypes.c_int64()
+        lat = ctypes.c_double()
+        _check(self._lib.emv_server_wait(self._srv, rid, ctypes.byref(cost), ctypes.byref(lat), timeout_s))
+        return int(cost.value), float(lat.value)
+
+    def cancel(self, rid: int) -> None:
+        _check(self._lib.emv_server_cancel(self._srv, rid))
+
+    def stats(self) -> dict:
+        s = _ServerStats()
+        _check(self._lib.emv_server_stats_get(self._srv, ctypes.byref(s)))
+        return {f: getattr(s, f) for f, _ in _ServerStats._fields_}
+
+    def close(self) -> None:
+        if self._srv:
+            self._lib.emv_server_destroy(self._srv)
+            self._srv = ctypes.c_void_p()
+
+    def __enter__(self) -> "Server":
+        return self
+
+    def __exit__(self, *exc) -> None:
+        self.close()
+
+
+# ------------------------------------------------- reference-named entry points
+
+def graph_load(path: Optional[str]) -> StpInstance:
+    """graph_load (R:473-618); None reads stdin."""
+    if path is None:
+        import sys
+        return StpInstance.from_text(sys.stdin.buffer.read())
+    return StpInstance.from_file(path)
+
+
+def root_build(g: StpInstance) -> Csr:
+    """root_build (R:706-899): CSR plus the terminal index kk."""
+    return Csr.from_stp(g)
+
+
+def erickson_monma_veinott(root: Csr, list_soln: bool = False, solver: Optional[Solver] = None) -> Result:
+    """erickson_monma_veinott (R:2141-2343) on the GPU."""
+    own = solver is None
+    s = Solver() if own else solver
+    try:
+        return s.solve(root, tree=list_soln)
+    finally:
+        if own:
+            s.close()
+
+
+def build() -> str:
+    """Compiles the native library and command in-tree (sm_103a)."""
+    return _build.build()

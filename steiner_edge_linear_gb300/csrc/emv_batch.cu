@@ -1,0 +1,367 @@
+// emv_batch.cu -- many independent instances in one persistent launch (C ABI),
+// and the autotuner that picks the per-class tile shapes.
+//
+// No counterpart in the reference, which solves one instance per process
+// (reader/reader-el.c:2355-2536); each instance's values are those of its
+// emv_kernel (R:1966-2139).
+#include "emv_batch.cuh"
+#include "emv_solver.h"
+#include "emv_batch_host.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+using namespace emv;
+
+namespace {
+
+int32_t pow2_floor(int32_t x)
+{
+    int32_t p = 1;
+    while (p * 2 <= x) p *= 2;
+    return p;
+}
+
+}  // namespace
+
+int32_t batch_class_of(int32_t n, int32_t k)
+{
+    const int32_t nb = n <= 256 ? 0 : n <= 1024 ? 1 : n <= 4096 ? 2 : 3;
+    const int32_t kb = k <= 6 ? 0 : k <= 8 ? 1 : 2;
+    return nb * 3 + kb;
+}
+
+// Largest rows-per-chunk whose vertex-major buffer fits the shared memory.
+int32_t batch_rcap_max(int32_t n)
+{
+    int32_t r = 32;
+    while (r > 1 && (int64_t)n * (r + 1) * 4 > BATCH_SMEM_BYTES) r /= 2;
+    return r;
+}
+
+bool batch_fits(int32_t n, int32_t k)
+{
+    return k >= 1 && k <= BATCH_KMAX && (int64_t)n * 2 * 4 <= BATCH_SMEM_BYTES &&
+           ((int64_t)32 << k) * 4 <= BATCH_SMEM_BYTES;
+}
+
+int32_t batch_rcap_for(const emv_ctx *c, int32_t n, int32_t k)
+{
+    const int32_t cap = batch_rcap_max(n);
+    const int32_t cls = batch_class_of(n, k);
+    int32_t r = (cls >= 0 && cls < BATCH_CLASSES && c->tune_rcap[cls] > 0) ? c->tune_rcap[cls] : 32;
+    return std::min(cap, pow2_floor(std::max(1, r)));
+}
+
+int prepare_batch_subsets(emv_ctx *c, cudaStream_t st)
+{
+    if (c->bxs_ready) return EMV_OK;
+    std::vector<uint32_t> all;
+    std::vector<int32_t> off((size_t)(BATCH_KMAX + 1) * (BATCH_KMAX + 2), 0);
+    for (int32_t k = 1; k <= BATCH_KMAX; k++) {
+        std::vector<uint32_t> xs;
+        std::vector<int64_t> lo;
+        subset_levels(k, xs, lo);
+        const int32_t base = (int32_t)all.size();
+        for (int32_t m = 0; m <= k + 1; m++) off[(size_t)k * (BATCH_KMAX + 2) + m] = base + (int32_t)lo[(size_t)m];
+        all.insert(all.end(), xs.begin(), xs.end());
+    }
+    int r = dev_reserve(c->bxs, sizeof(uint32_t) * all.size());
+    if (!r) r = dev_reserve(c->bxs_off, sizeof(int32_t) * off.size());
+    if (r) return r;
+    CUDA_TRY(cudaMemcpyAsync(c->bxs.ptr, all.data(), sizeof(uint32_t) * all.size(), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(c->bxs_off.ptr, off.data(), sizeof(int32_t) * off.size(), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    c->bxs_ready = true;
+    return EMV_OK;
+}
+
+int batch_kernel_setup(emv_ctx *c)
+{
+    if (c->batch_blocks > 0) return EMV_OK;
+    CUDA_TRY(cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, BATCH_SMEM_BYTES));
+    int per_sm = 0;
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, BATCH_THREADS, BATCH_SMEM_BYTES));
+    c->batch_blocks = std::max(1, per_sm) * c->sms;
+    return EMV_OK;
+}
+
+// Launches k_batch over `count` prepared descriptors (device arrays already set).
+int launch_batch(emv_ctx *c, const BatchArgs &args, int32_t count, cudaStream_t st)
+{
+    int r = batch_kernel_setup(c);
+    if (r) return r;
+    CUDA_TRY(cudaMemsetAsync(args.queue, 0, sizeof(uint32_t), st));
+    const int blocks = std::min(c->batch_blocks, std::max(1, count));
+    BatchArgs a = args;
+    k_batch<<<blocks, BATCH_THREADS, BATCH_SMEM_BYTES, st>>>(a);
+    CUDA_TRY(cudaGetLastError());
+    return EMV_OK;
+}
+
+// Estimated device work of one instance, for largest-first ordering.
+double batch_work(int32_t n, int32_t k, int64_t arcs)
+{
+    return std::pow(3.0, k) * n * 0.5 + std::pow(2.0, k) * (double)arcs * 6.0;
+}
+
+extern "C" int emv_batch_solve(emv_ctx *c, const emv_instance *inst, int32_t count, int64_t *costs_out,
+                               emv_batch_stats *stats, void *stream)
+{
+    if (!c || (count > 0 && (!inst || !costs_out)) || count < 0)
+        return emv_fail(EMV_ERR_BAD_INPUT, "emv_batch_solve: bad arguments");
+    if (count == 0) return EMV_OK;
+    CUDA_TRY(cudaSetDevice(c->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    const auto t0 = std::chrono::steady_clock::now();
+    for (int32_t i = 0; i < count; i++) {
+        const emv_instance &I = inst[i];
+        int r = emv_graph_validate(&I.g);
+        if (r) return emv_fail(r, "instance %d: %s", i, emv_last_error());
+        if (!batch_fits(I.g.n, I.k))
+            return emv_fail(EMV_ERR_BAD_INPUT, "instance %d: n = %d, k = %d outside the batched range (k <= %d)", i,
+                            I.g.n, I.k, BATCH_KMAX);
+        if (!I.terminals) return emv_fail(EMV_ERR_BAD_INPUT, "instance %d: null terminals", i);
+        for (int32_t t = 0; t < I.k; t++)
+            if (I.terminals[t] < 0 || I.terminals[t] >= I.g.n)
+                return emv_fail(EMV_ERR_BAD_INPUT, "instance %d: terminal out of range", i);
+        r = emv_graph_check(&I.g, nullptr);
+        if (r) return emv_fail(r, "instance %d: %s", i, emv_last_error());
+    }
+    // Largest first, so the persistent CTAs finish together.
+    std::vector<int32_t> order((size_t)count);
+    for (int32_t i = 0; i < count; i++) order[(size_t)i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) {
+        return batch_work(inst[x].g.n, inst[x].k, inst[x].g.arcs) > batch_work(inst[y].g.n, inst[y].k, inst[y].g.arcs);
+    });
+    BatchPack pk;
+    int r = batch_pack(c, inst, order, 1, -1, pk);
+    if (r) return r;
+    r = batch_upload(c, pk, st);
+    if (r) return r;
+    CUDA_TRY(cudaEventRecord(c->ev[0], st));
+    BatchArgs a = batch_args(c, pk);
+    // The queue reset and the persistent launch are replayed as one CUDA graph.
+    r = batch_graph_launch(c, a, count, st);
+    if (r) return r;
+    CUDA_TRY(cudaEventRecord(c->ev[1], st));
+    CUDA_TRY(cudaMemcpyAsync(costs_out, a.costs, sizeof(int64_t) * (size_t)count, cudaMemcpyDeviceToHost, st));
+    uint32_t err = 0;
+    CUDA_TRY(cudaMemcpyAsync(&err, a.err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    if (err) return emv_dev_status_to_emv(err);
+    if (stats) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
+        stats->total_ms = ms;
+        stats->upload_ms = (float)std::chrono::duration<double, std::milli>(pk.t_upload_end - t0).count();
+        stats->work_items = count;
+        stats->table_bytes = pk.table_words * 4;
+        stats->merge_tile = 32;
+        stats->relax_rows = pk.rcap_used;
+    }
+    return EMV_OK;
+}
+
+// ---------------------------------------------------------------- packing
+
+int batch_pack(emv_ctx *c, const emv_instance *inst, const std::vector<int32_t> &order, int32_t lo, int32_t hi,
+               BatchPack &pk)
+{
+    const int32_t count = (int32_t)order.size();
+    pk.desc.resize((size_t)count);
+    int64_t rows = 0, arcs = 0, terms = 0, words = 0;
+    for (int32_t j = 0; j < count; j++) {
+        const emv_instance &I = inst[order[(size_t)j]];
+        BatchInst &d = pk.desc[(size_t)j];
+        d.n = I.g.n;
+        d.k = I.k;
+        d.rcap = batch_rcap_for(c, I.g.n, I.k);
+        d.orig = order[(size_t)j];
+        d.row_off = rows;
+        d.arc_off = arcs;
+        d.table_off = words;
+        d.term_off = (int32_t)terms;
+        d.lo = lo;
+        d.hi = hi < 0 ? I.k : hi;
+        d.pad = 0;
+        rows += I.g.n + 1;
+        arcs += I.g.arcs;
+        terms += I.k;
+        words += ((int64_t)I.g.n << I.k);
+        pk.rcap_used = std::max(pk.rcap_used, d.rcap);
+    }
+    pk.rows = rows;
+    pk.arcs = arcs;
+    pk.terms = terms;
+    pk.table_words = words;
+    pk.count = count;
+    // Host staging (pinned, reused): row_ptr | adj | terms | desc
+    const size_t bytes = sizeof(int32_t) * (size_t)rows + sizeof(int2) * (size_t)arcs + sizeof(int32_t) * (size_t)terms +
+                         sizeof(BatchInst) * (size_t)count + 64;
+    if (c->bstage_bytes < bytes) {
+        if (c->bstage) cudaFreeHost(c->bstage);
+        c->bstage = nullptr;
+        c->bstage_bytes = 0;
+        if (cudaMallocHost(&c->bstage, bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return emv_fail(EMV_ERR_OOM, "pinned staging of %zu bytes", bytes);
+        }
+        c->bstage_bytes = bytes;
+    }
+    char *p = (char *)c->bstage;
+    int32_t *hrow = (int32_t *)p;
+    int2 *hadj = (int2 *)(hrow + rows);
+    int32_t *hterm = (int32_t *)(hadj + arcs);
+    BatchInst *hdesc = (BatchInst *)(((uintptr_t)(hterm + terms) + 15) & ~(uintptr_t)15);
+    for (int32_t j = 0; j < count; j++) {
+        const emv_instance &I = inst[order[(size_t)j]];
+        const BatchInst &d = pk.desc[(size_t)j];
+        std::memcpy(hrow + d.row_off, I.g.row_ptr, sizeof(int32_t) * ((size_t)I.g.n + 1));
+        for (int64_t e = 0; e < I.g.arcs; e++) hadj[d.arc_off + e] = make_int2(I.g.col[e], I.g.w[e]);
+        std::memcpy(hterm + d.term_off, I.terminals, sizeof(int32_t) * (size_t)I.k);
+    }
+    std::memcpy(hdesc, pk.desc.data(), sizeof(BatchInst) * (size_t)count);
+    pk.h_row = hrow;
+    pk.h_adj = hadj;
+    pk.h_term = hterm;
+    pk.h_desc = hdesc;
+    return EMV_OK;
+}
+
+int batch_upload(emv_ctx *c, BatchPack &pk, cudaStream_t st)
+{
+    int r = dev_reserve(c->b_row, sizeof(int32_t) * (size_t)pk.rows);
+    if (!r) r = dev_reserve(c->b_adj, sizeof(int2) * (size_t)std::max<int64_t>(pk.arcs, 1));
+    if (!r) r = dev_reserve(c->b_term, sizeof(int32_t) * (size_t)std::max<int64_t>(pk.terms, 1));
+    if (!r) r = dev_reserve(c->b_desc, sizeof(BatchInst) * (size_t)pk.count);
+    if (!r) r = dev_reserve(c->b_table, sizeof(int32_t) * (size_t)pk.table_words);
+    if (!r) r = dev_reserve(c->b_costs, sizeof(int64_t) * (size_t)pk.count);
+    if (!r) r = dev_reserve(c->b_ctrl, 64);
+    if (!r) r = prepare_batch_subsets(c, st);
+    if (r) return r;
+    CUDA_TRY(cudaMemcpyAsync(c->b_row.ptr, pk.h_row, sizeof(int32_t) * (size_t)pk.rows, cudaMemcpyHostToDevice, st));
+    if (pk.arcs > 0)
+        CUDA_TRY(cudaMemcpyAsync(c->b_adj.ptr, pk.h_adj, sizeof(int2) * (size_t)pk.arcs, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(c->b_term.ptr, pk.h_term, sizeof(int32_t) * (size_t)pk.terms, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(c->b_desc.ptr, pk.h_desc, sizeof(BatchInst) * (size_t)pk.count, cudaMemcpyHostToDevice,
+                             st));
+    CUDA_TRY(cudaMemsetAsync(c->b_ctrl.ptr, 0, 64, st));
+    pk.t_upload_end = std::chrono::steady_clock::now();
+    return EMV_OK;
+}
+
+BatchArgs batch_args(emv_ctx *c, const BatchPack &pk)
+{
+    BatchArgs a;
+    std::memset(&a, 0, sizeof(a));  // padding included: the graph cache compares bytes
+    a.inst = (const BatchInst *)c->b_desc.ptr;
+    a.count = pk.count;
+    a.row_ptr = (const int32_t *)c->b_row.ptr;
+    a.adj = (const int2 *)c->b_adj.ptr;
+    a.terms = (const int32_t *)c->b_term.ptr;
+    a.tables = (int32_t *)c->b_table.ptr;
+    a.xs = (const uint32_t *)c->bxs.ptr;
+    a.xs_off = (const int32_t *)c->bxs_off.ptr;
+    a.costs = (int64_t *)c->b_costs.ptr;
+    a.queue = (uint32_t *)c->b_ctrl.ptr;
+    a.err = (uint32_t *)c->b_ctrl.ptr + 8;
+    return a;
+}
+
+// Captures {queue reset, persistent kernel} once per argument set and replays it.
+int batch_graph_launch(emv_ctx *c, const BatchArgs &a, int32_t count, cudaStream_t st)
+{
+    int r = batch_kernel_setup(c);
+    if (r) return r;
+    static_assert(sizeof(BatchArgs) <= sizeof(c->bgraph_args), "graph key too small");
+    const bool same = c->bgraph_exec && std::memcmp(c->bgraph_args, &a, sizeof(a)) == 0;
+    if (!same) {
+        if (c->bgraph_exec) cudaGraphExecDestroy(c->bgraph_exec);
+        c->bgraph_exec = nullptr;
+        cudaStream_t cap;
+        CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            r = launch_batch(c, a, count, cap);
+            e = cudaStreamEndCapture(cap, &g);
+        }
+        cudaStreamDestroy(cap);
+        if (r) return r;
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return emv_fail(EMV_ERR_CUDA, "batch graph capture: %s", cudaGetErrorString(e));
+        }
+        e = cudaGraphInstantiate(&c->bgraph_exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            c->bgraph_exec = nullptr;
+            return emv_fail(EMV_ERR_CUDA, "batch graph instantiate: %s", cudaGetErrorString(e));
+        }
+        std::memcpy(c->bgraph_args, &a, sizeof(a));
+    }
+    CUDA_TRY(cudaGraphLaunch(c->bgraph_exec, st));
+    return EMV_OK;
+}
+
+// --------------------------------------------------------------- autotuner
+
+// For every instance class present in `inst`, times the candidate
+// rows-per-chunk values of the relaxation on a sample of that class and keeps
+// the fastest in the context (and in *out_rcap[class] when given).
+extern "C" int emv_batch_autotune(emv_ctx *c, const emv_instance *inst, int32_t count, int32_t *out_rcap,
+                                  void *stream)
+{
+    if (!c || (count > 0 && !inst)) return emv_fail(EMV_ERR_BAD_INPUT, "emv_batch_autotune: bad arguments");
+    CUDA_TRY(cudaSetDevice(c->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    std::vector<std::vector<int32_t>> by_class(BATCH_CLASSES);
+    for (int32_t i = 0; i < count; i++) {
+        if (!batch_fits(inst[i].g.n, inst[i].k)) continue;
+        const int32_t cls = batch_class_of(inst[i].g.n, inst[i].k);
+        if (by_class[(size_t)cls].size() < 64) by_class[(size_t)cls].push_back(i);
+    }
+    for (int32_t cls = 0; cls < BATCH_CLASSES; cls++) {
+        auto &ids = by_class[(size_t)cls];
+        if (ids.empty()) continue;
+        float best_ms = 1e30f;
+        int32_t best = 0;
+        for (int32_t cand : {4, 8, 16, 32}) {
+            c->tune_rcap[cls] = cand;
+            BatchPack pk;
+            int r = batch_pack(c, inst, ids, 1, -1, pk);
+            if (!r) r = batch_upload(c, pk, st);
+            if (r) return r;
+            BatchArgs a = batch_args(c, pk);
+            float ms = 0;
+            for (int rep = 0; rep < 2; rep++) {
+                CUDA_TRY(cudaEventRecord(c->ev[0], st));
+                r = launch_batch(c, a, pk.count, st);
+                if (r) return r;
+                CUDA_TRY(cudaEventRecord(c->ev[1], st));
+                CUDA_TRY(cudaStreamSynchronize(st));
+                cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
+            }
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = cand;
+            }
+        }
+        c->tune_rcap[cls] = best;
+    }
+    if (out_rcap)
+        for (int32_t cls = 0; cls < BATCH_CLASSES; cls++) out_rcap[cls] = c->tune_rcap[cls];
+    return EMV_OK;
+}
+
+extern "C" int emv_batch_set_tuning(emv_ctx *c, const int32_t *rcap, int32_t classes)
+{
+    if (!c || !rcap || classes != BATCH_CLASSES) return emv_fail(EMV_ERR_BAD_INPUT, "emv_batch_set_tuning: bad arguments");
+    for (int32_t i = 0; i < classes; i++) c->tune_rcap[i] = rcap[i];
+    return EMV_OK;
+}

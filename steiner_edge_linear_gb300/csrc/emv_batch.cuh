@@ -1,0 +1,203 @@
+// emv_batch.cuh -- the CTA-resident EMV solver used by batching and serving.
+//
+// One CTA owns one instance at a time and runs a window of its DP levels with
+// CTA barriers only, so no grid-wide synchronisation is needed and thousands
+// of independent instances of uneven n and k share one persistent launch.
+// Per level m of an instance (reader/reader-el.c:2033-2131):
+//   merge  -- vertex blocks of 32: every row of size < m is staged in shared
+//             memory as S[Y][32], a warp computes one subset X at a time with
+//             a lane per vertex (R:2068-2107);
+//   relax  -- chunks of R rows are loaded into shared memory vertex-major
+//             (stride R+1, conflict-free), and in-place sweeps pull
+//             min(d[u] + w) over the CSR until a sweep changes nothing
+//             (R:2109-2130), then the rows go back to the table.
+// The table of an instance is int32 row-major with ld = n.
+#pragma once
+
+#include "emv_common.cuh"
+
+namespace emv {
+
+constexpr int BATCH_THREADS = 1024;
+constexpr int BATCH_KMAX = 12;
+constexpr int32_t BATCH_SMEM_BYTES = 200 * 1024;
+
+struct BatchInst {
+    int32_t n;
+    int32_t k;
+    int32_t rcap;       // relaxation rows per chunk (autotuned, power of two <= 32)
+    int32_t orig;       // position in the caller's order
+    int64_t row_off;    // into BatchArgs::row_ptr (n + 1 entries, 0-based arcs)
+    int64_t arc_off;    // into BatchArgs::adj
+    int64_t table_off;  // into BatchArgs::tables (int32 units)
+    int32_t term_off;   // into BatchArgs::terms
+    int32_t lo;         // first level to run (1..k)
+    int32_t hi;         // last level to run (lo..k)
+    int32_t pad;
+};
+
+struct BatchArgs {
+    const BatchInst *inst;
+    int32_t count;
+    const int32_t *row_ptr;
+    const int2 *adj;
+    const int32_t *terms;
+    int32_t *tables;
+    const uint32_t *xs;      // subsets by level for k = 1..BATCH_KMAX, concatenated
+    const int32_t *xs_off;   // xs_off[k * (BATCH_KMAX + 2) + m]: start of level m of k
+    int64_t *costs;          // by orig; written when hi == k
+    uint32_t *queue;         // [0] next work item
+    uint32_t *err;
+};
+
+__device__ __forceinline__ int32_t xs_start(const BatchArgs &a, int32_t k, int32_t m)
+{
+    return __ldg(a.xs_off + k * (BATCH_KMAX + 2) + m);
+}
+
+// Merge of level m for one instance; S holds 2^k * 32 int32.
+__device__ void batch_merge(const BatchArgs &a, int32_t *table, int32_t n, int32_t k, int32_t m,
+                            const int32_t *terms, int32_t *S)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int32_t lo_b = xs_start(a, k, 1), lo_e = xs_start(a, k, m);       // rows of size 1..m-1
+    const int32_t x_b = xs_start(a, k, m), x_e = xs_start(a, k, m + 1);     // rows of size m
+    const uint32_t *xs = a.xs;
+    for (int32_t vb = 0; vb < n; vb += 32) {
+        const int32_t v = vb + lane;
+        for (int32_t i = lo_b + warp; i < lo_e; i += nw) {
+            const uint32_t Y = __ldg(xs + i);
+            S[Y * 32 + lane] = (v < n) ? table[(int64_t)Y * n + v] : INF;
+        }
+        __syncthreads();
+        if (v < n) {
+            for (int32_t i = x_b + warp; i < x_e; i += nw) {
+                const uint32_t X = __ldg(xs + i);
+                const uint32_t low = X & (0u - X), rest = X ^ low;
+                uint32_t acc = (uint32_t)INF;
+                uint32_t s = 0;
+                do {
+                    const uint32_t Y = low | s;
+                    acc = min(acc, (uint32_t)S[Y * 32 + lane] + (uint32_t)S[(X ^ Y) * 32 + lane]);
+                    s = (s - rest) & rest;
+                } while (s != rest);
+                for (uint32_t bits = X; bits; bits &= bits - 1) {
+                    const int t = __ffs(bits) - 1;
+                    if (terms[t] == v) acc = (uint32_t)S[(X ^ (1u << t)) * 32 + lane];
+                }
+                table[(int64_t)X * n + v] = (int32_t)acc;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Closure of the rows xs[b, e) (level-1 mode: row r is {r} with source terms[r]).
+// Returns false if the sweep bound was hit.
+__device__ bool batch_relax(const BatchArgs &a, int32_t *table, int32_t n, const int32_t *row_ptr, const int2 *adj,
+                            const int32_t *terms, int32_t b, int32_t e, int32_t rcap, bool level1, int32_t *S)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int32_t cnt = e - b;
+    int32_t R = 1;
+    while (R < cnt && R < rcap) R <<= 1;
+    const int32_t stride = R + 1;
+    const int32_t G = 32 / R;              // vertices per warp task
+    const int32_t vs = lane / R, r = lane % R;
+    bool ok = true;
+    for (int32_t c0 = 0; c0 < cnt; c0 += R) {
+        const int32_t nr = min(R, cnt - c0);
+        for (int32_t idx = threadIdx.x; idx < R * n; idx += blockDim.x) {
+            const int32_t rr = idx / n, v = idx - rr * n;
+            int32_t x = INF;
+            if (rr < nr) {
+                if (level1) x = (v == terms[c0 + rr]) ? 0 : INF;
+                else x = table[(int64_t)__ldg(a.xs + b + c0 + rr) * n + v];
+            }
+            S[v * stride + rr] = x;
+        }
+        __syncthreads();
+        const int32_t tasks = (n + G - 1) / G;
+        int32_t sweep = 0;
+        for (;; sweep++) {
+            if (sweep > n + 1) { ok = false; break; }
+            bool changed = false;
+            for (int32_t t = warp; t < tasks; t += nw) {
+                const int32_t v = t * G + vs;
+                if (v < n && r < nr) {
+                    const int32_t beg = __ldg(row_ptr + v), end = __ldg(row_ptr + v + 1);
+                    const int32_t old = S[v * stride + r];
+                    int32_t acc = old;
+                    for (int32_t q = beg; q < end; q++) {
+                        const int2 arc = __ldg(adj + q);
+                        acc = min(acc, S[arc.x * stride + r] + arc.y);
+                    }
+                    if (acc < old) {
+                        S[v * stride + r] = acc;
+                        changed = true;
+                    }
+                }
+            }
+            if (!__syncthreads_or(changed)) break;
+        }
+        for (int32_t idx = threadIdx.x; idx < nr * n; idx += blockDim.x) {
+            const int32_t rr = idx / n, v = idx - rr * n;
+            table[(int64_t)__ldg(a.xs + b + c0 + rr) * n + v] = S[v * stride + rr];
+        }
+        __syncthreads();
+        if (!ok) break;
+    }
+    return ok;
+}
+
+// Runs levels [lo, hi] of one instance with the whole CTA.
+__device__ void batch_solve_one(const BatchArgs &a, const BatchInst &I, int32_t *S)
+{
+    const int32_t n = I.n, k = I.k;
+    int32_t *table = a.tables + I.table_off;
+    const int32_t *row_ptr = a.row_ptr + I.row_off;
+    const int2 *adj = a.adj + I.arc_off;
+    const int32_t *terms = a.terms + I.term_off;
+    bool ok = true;
+    for (int32_t m = I.lo; m <= I.hi && ok; m++) {
+        if (m == 1) {
+            for (int32_t v = threadIdx.x; v < n; v += blockDim.x) table[v] = INF;  // row 0
+            ok = batch_relax(a, table, n, row_ptr, adj, terms, xs_start(a, k, 1), xs_start(a, k, 2), I.rcap, true, S);
+        } else {
+            batch_merge(a, table, n, k, m, terms, S);
+            ok = batch_relax(a, table, n, row_ptr, adj, terms, xs_start(a, k, m), xs_start(a, k, m + 1), I.rcap,
+                             false, S);
+        }
+    }
+    if (threadIdx.x == 0) {
+        if (!ok) atomicOr(a.err, (uint32_t)EMV_DEV_SWEEP_LIMIT);
+        if (I.hi == k) {
+            int64_t cost = INT64_MAX;
+            if (k >= 2) {
+                const int32_t x = table[(int64_t)((1 << (k - 1)) - 1) * n + terms[k - 1]];
+                if (x < INF) cost = x;
+            }
+            a.costs[I.orig] = cost;
+        }
+    }
+}
+
+// Persistent kernel: CTAs pull work items (instances in the given order,
+// largest first) from a device counter until the queue is empty.
+__global__ void __launch_bounds__(BATCH_THREADS, 1) k_batch(BatchArgs a)
+{
+    extern __shared__ int32_t S[];
+    __shared__ int32_t s_idx;
+    for (;;) {
+        if (threadIdx.x == 0) s_idx = (int32_t)atomicAdd(a.queue, 1u);
+        __syncthreads();
+        const int32_t idx = s_idx;
+        __syncthreads();
+        if (idx >= a.count) break;
+        const BatchInst I = a.inst[idx];
+        batch_solve_one(a, I, S);
+        __syncthreads();
+    }
+}
+
+}  // namespace emv

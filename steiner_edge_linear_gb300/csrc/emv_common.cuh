@@ -1,0 +1,28 @@
+// emv_common.cuh -- constants and status words shared by every kernel file.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "emv_internal.h"
+
+namespace emv {
+
+constexpr int32_t INF = EMV_INF32;
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int RELAX_THREADS = 256;       // 8 warps, one vertex per warp at a time
+constexpr int CHUNK_ROWS = 32;           // rows per relaxation chunk, one per lane
+constexpr uint32_t SPIN_LIMIT = 1u << 22;  // grid-barrier spin iterations (~1 s with nanosleep)
+constexpr int TB_STACK = 64;
+
+// ctrl words of one cooperative relaxation launch (zeroed before the launch)
+enum : int { C_BAR_COUNT = 0, C_BAR_GEN = 1, C_ERR = 2, C_SLOT0 = 4, C_WORDS = 8 };
+
+// Persistent device status of one solve (zeroed at solve start).
+struct DevStat {
+    uint32_t err;
+    uint32_t pad;
+    unsigned long long sweeps;
+};
+
+}  // namespace emv

@@ -1,0 +1,477 @@
+// emv_device.cu -- solver context and the single-instance GPU DP (C ABI).
+//
+// Reference counterparts (reader/reader-el.c):
+//   emv_kernel              R:1966-2139  -> emv_kernel_dev
+//   erickson_monma_veinott  R:2141-2343  -> emv_solve / emv_solve_dev
+//   dijkstra (-dijkstra)    R:1762-1880, R:2454-2484 -> emv_sssp
+#include "emv_kernels.cuh"
+#include "emv_solver.h"
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+using namespace emv;
+
+int emv_dev_status_to_emv(uint32_t s)
+{
+    if (s == 0) return EMV_OK;
+    if (s & (EMV_DEV_BARRIER_TIMEOUT | EMV_DEV_SWEEP_LIMIT | EMV_DEV_TB_STEPS | EMV_DEV_QUEUE_TIMEOUT))
+        return emv_fail(EMV_ERR_TIMEOUT, "device loop bound reached (status 0x%x)", s);
+    return emv_fail(EMV_ERR_INTERNAL, "device status 0x%x", s);
+}
+
+extern "C" const char *emv_version(void) { return "emv-gb300 1.0 sm_103a"; }
+
+// ------------------------------------------------------------ buffers
+
+int dev_reserve(DevBuf &b, size_t bytes)
+{
+    if (b.bytes >= bytes) return EMV_OK;
+    if (b.ptr) cudaFree(b.ptr);
+    b.ptr = nullptr;
+    b.bytes = 0;
+    size_t want = std::max<size_t>(bytes, 256);
+    cudaError_t e = cudaMalloc(&b.ptr, want);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        b.ptr = nullptr;
+        return emv_fail(e == cudaErrorMemoryAllocation ? EMV_ERR_OOM : EMV_ERR_CUDA,
+                        "cudaMalloc(%zu): %s", want, cudaGetErrorString(e));
+    }
+    b.bytes = want;
+    return EMV_OK;
+}
+
+void dev_release(DevBuf &b)
+{
+    if (b.ptr) cudaFree(b.ptr);
+    b.ptr = nullptr;
+    b.bytes = 0;
+}
+
+// ------------------------------------------------------------ subsets
+
+// All non-empty subsets of {0..k-1} grouped by size, increasing within a
+// size -- the order Gosper's hack gives each level (R:2041-2046).
+void subset_levels(int32_t k, std::vector<uint32_t> &xs, std::vector<int64_t> &off)
+{
+    const uint32_t rows = 1u << k;
+    off.assign((size_t)k + 2, 0);
+    for (uint32_t X = 1; X < rows; X++) off[(size_t)__builtin_popcount(X) + 1]++;
+    for (int32_t m = 1; m <= k; m++) off[(size_t)m + 1] += off[(size_t)m];
+    xs.resize(rows - 1);
+    std::vector<int64_t> fill(off.begin(), off.end());
+    for (uint32_t X = 1; X < rows; X++) xs[(size_t)fill[(size_t)__builtin_popcount(X)]++] = X;
+}
+
+// ------------------------------------------------------------ context
+
+extern "C" int emv_create(emv_ctx **out, int32_t device)
+{
+    if (!out) return emv_fail(EMV_ERR_BAD_INPUT, "null ctx pointer");
+    *out = nullptr;
+    int ndev = 0;
+    CUDA_TRY(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) return emv_fail(EMV_ERR_BAD_INPUT, "device %d of %d", device, ndev);
+    CUDA_TRY(cudaSetDevice(device));
+    cudaDeviceProp prop;
+    CUDA_TRY(cudaGetDeviceProperties(&prop, device));
+    if (!prop.cooperativeLaunch) return emv_fail(EMV_ERR_CUDA, "device lacks cooperative launch");
+    emv_ctx *c = new (std::nothrow) emv_ctx();
+    if (!c) return emv_fail(EMV_ERR_OOM, "ctx");
+    c->device = device;
+    c->sms = prop.multiProcessorCount;
+    int per_sm = 0;
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_relax_chunk, RELAX_THREADS, 0));
+    c->relax_blocks_max = std::max(1, per_sm) * c->sms;
+    int st = dev_reserve(c->ctrl, sizeof(uint32_t) * C_WORDS);
+    if (!st) st = dev_reserve(c->stat, sizeof(DevStat));
+    if (!st) {
+        if (cudaMallocHost(&c->pinned, 4096) != cudaSuccess) { cudaGetLastError(); st = emv_fail(EMV_ERR_OOM, "pinned"); }
+    }
+    for (int i = 0; !st && i < MAX_EVENTS; i++)
+        if (cudaEventCreate(&c->ev[i]) != cudaSuccess) st = emv_fail(EMV_ERR_CUDA, "event create");
+    if (st) {
+        emv_destroy(c);
+        return st;
+    }
+    *out = c;
+    return EMV_OK;
+}
+
+extern "C" int emv_destroy(emv_ctx *c)
+{
+    if (!c) return EMV_OK;
+    cudaSetDevice(c->device);
+    cudaDeviceSynchronize();
+    for (DevBuf *b : {&c->ctrl, &c->stat, &c->scratch, &c->act, &c->adj, &c->xs, &c->terms, &c->g_row,
+                      &c->g_col, &c->g_w, &c->table, &c->tb_edges, &c->tb_out, &c->tb_work})
+        dev_release(*b);
+    for (int i = 0; i < MAX_EVENTS; i++)
+        if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+    if (c->pinned) cudaFreeHost(c->pinned);
+    delete c;
+    return EMV_OK;
+}
+
+// ------------------------------------------------------------ the DP
+
+static int grid_for(int64_t work, int threads, int cap)
+{
+    int64_t g = (work + threads - 1) / threads;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(g, cap));
+}
+
+// Launches the relaxation of one chunk of rows (cooperative, persistent).
+int launch_relax(emv_ctx *c, const int32_t *row_ptr, const int2 *adj, int32_t n, int64_t ld, int32_t *table,
+                 const uint32_t *rows, int32_t nrows, const int32_t *terms, int32_t level1, cudaStream_t st)
+{
+    RelaxArgs a;
+    a.row_ptr = row_ptr;
+    a.adj = adj;
+    a.n = n;
+    a.ld = ld;
+    a.table = table;
+    a.rows = rows;
+    a.nrows = nrows;
+    a.terms = terms;
+    a.level1 = level1;
+    a.scratch = (int32_t *)c->scratch.ptr;
+    a.act0 = (uint8_t *)c->act.ptr;
+    a.act1 = (uint8_t *)c->act.ptr + ((size_t)n + 255) / 256 * 256;
+    a.ctrl = (uint32_t *)c->ctrl.ptr;
+    a.stat = (DevStat *)c->stat.ptr;
+    a.max_sweeps = n + 1;
+    // One warp per vertex is enough; small graphs use fewer blocks (cheaper barriers).
+    const int blocks = std::min(c->relax_blocks_max, std::max(1, (n + 7) / 8));
+    CUDA_TRY(cudaMemsetAsync(a.ctrl, 0, sizeof(uint32_t) * C_WORDS, st));
+    void *args[] = {&a};
+    CUDA_TRY(cudaLaunchCooperativeKernel((const void *)k_relax_chunk, dim3(blocks), dim3(RELAX_THREADS), args, 0, st));
+    k_collect_err<<<1, 32, 0, st>>>(a.ctrl, a.stat);
+    c->launches += 3;
+    return EMV_OK;
+}
+
+int reserve_relax(emv_ctx *c, int32_t n)
+{
+    const size_t npad = ((size_t)n + 31) / 32 * 32;
+    int st = dev_reserve(c->scratch, npad * CHUNK_ROWS * sizeof(int32_t));
+    if (!st) st = dev_reserve(c->act, 2 * (((size_t)n + 255) / 256 * 256));
+    return st;
+}
+
+int prepare_subsets(emv_ctx *c, int32_t k, cudaStream_t st)
+{
+    if (c->xs_k == k) return EMV_OK;
+    subset_levels(k, c->xs_host, c->xs_off);
+    int r = dev_reserve(c->xs, sizeof(uint32_t) * std::max<size_t>(1, c->xs_host.size()));
+    if (r) return r;
+    CUDA_TRY(cudaMemcpyAsync(c->xs.ptr, c->xs_host.data(), sizeof(uint32_t) * c->xs_host.size(),
+                             cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    c->xs_k = k;
+    return EMV_OK;
+}
+
+// The DP proper on device data with packed arcs; fills the whole table.
+int run_dp(emv_ctx *c, int32_t n, const int32_t *row_ptr, const int2 *adj, int32_t k, const int32_t *terms_host,
+           int32_t *table, int64_t ld, cudaStream_t st, int64_t *cost_out, emv_timing *tm)
+{
+    int r = prepare_subsets(c, k, st);
+    if (!r) r = reserve_relax(c, n);
+    if (!r) r = dev_reserve(c->terms, sizeof(int32_t) * (size_t)k);
+    if (r) return r;
+    int32_t *d_terms = (int32_t *)c->terms.ptr;
+    CUDA_TRY(cudaMemcpyAsync(d_terms, terms_host, sizeof(int32_t) * (size_t)k, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemsetAsync(c->stat.ptr, 0, sizeof(DevStat), st));
+    const uint32_t *xs = (const uint32_t *)c->xs.ptr;
+    int ev = 0;
+    cudaEvent_t *E = c->ev;
+    CUDA_TRY(cudaEventRecord(E[ev++], st));  // 0: start
+
+    // Row 0 is the only row no level writes (R:2243-2259 fills every row).
+    k_fill<<<grid_for(n, 256, 1024), 256, 0, st>>>(table, n, INF);
+    c->launches++;
+    CUDA_TRY(cudaEventRecord(E[ev++], st));  // 1: after fill
+
+    // Level 1: k single-source closures (R:1988-2031).
+    r = launch_relax(c, row_ptr, adj, n, ld, table, xs + c->xs_off[1], k, d_terms, 1, st);
+    if (r) return r;
+    CUDA_TRY(cudaEventRecord(E[ev++], st));  // 2: after level 1
+
+    for (int32_t m = 2; m <= k; m++) {
+        const int64_t b = c->xs_off[(size_t)m], cnt = c->xs_off[(size_t)m + 1] - b;
+        const int32_t xper = (int32_t)std::min<int64_t>(cnt, 64);
+        dim3 grid((unsigned)((n + 31) / 32), (unsigned)((cnt + xper - 1) / xper));
+        k_merge<<<grid, 256, 0, st>>>(table, ld, n, xs + b, (int32_t)cnt, xper, d_terms, k);
+        c->launches++;
+        CUDA_TRY(cudaGetLastError());
+        CUDA_TRY(cudaEventRecord(E[ev++], st));  // merge end of level m
+        for (int64_t off = 0; off < cnt; off += CHUNK_ROWS) {
+            const int32_t rows = (int32_t)std::min<int64_t>(CHUNK_ROWS, cnt - off);
+            r = launch_relax(c, row_ptr, adj, n, ld, table, xs + b + off, rows, d_terms, 0, st);
+            if (r) return r;
+        }
+        CUDA_TRY(cudaEventRecord(E[ev++], st));  // relax end of level m
+    }
+
+    // Cost d[C][q] (R:2137-2138) and the device status, then one host sync.
+    int32_t *hp = (int32_t *)c->pinned;
+    if (k >= 2) {
+        const int64_t C = ((int64_t)1 << (k - 1)) - 1;
+        CUDA_TRY(cudaMemcpyAsync(hp, table + C * ld + terms_host[k - 1], sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    } else {
+        hp[0] = INF;
+    }
+    CUDA_TRY(cudaMemcpyAsync(hp + 2, c->stat.ptr, sizeof(DevStat), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    CUDA_TRY(cudaGetLastError());
+    DevStat ds;
+    std::memcpy(&ds, hp + 2, sizeof(ds));
+    if (ds.err) return emv_dev_status_to_emv(ds.err);
+    *cost_out = (k >= 2 && hp[0] < INF) ? (int64_t)hp[0] : INT64_MAX;
+    if (tm) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, E[0], E[1]);
+        tm->zero_ms = ms;
+        cudaEventElapsedTime(&ms, E[1], E[2]);
+        tm->level1_ms = ms;
+        tm->merge_ms = tm->relax_ms = 0;
+        for (int32_t m = 2; m <= k; m++) {
+            const int b = 2 + 2 * (m - 2);  // E[b] merge start, E[b+1] relax start, E[b+2] level end
+            cudaEventElapsedTime(&ms, E[b], E[b + 1]);
+            tm->merge_ms += ms;
+            cudaEventElapsedTime(&ms, E[b + 1], E[b + 2]);
+            tm->relax_ms += ms;
+        }
+        cudaEventElapsedTime(&ms, E[1], E[ev - 1]);
+        tm->kernel_ms = ms;
+        tm->relax_sweeps = (int64_t)ds.sweeps;
+    }
+    return EMV_OK;
+}
+
+static int check_k(int32_t n, int32_t k, const int32_t *terms)
+{
+    if (k < 1 || k > EMV_MAX_K) return emv_fail(EMV_ERR_BAD_INPUT, "k = %d outside [1, %d]", k, EMV_MAX_K);
+    if (!terms) return emv_fail(EMV_ERR_BAD_INPUT, "null terminals");
+    for (int32_t i = 0; i < k; i++)
+        if (terms[i] < 0 || terms[i] >= n) return emv_fail(EMV_ERR_BAD_INPUT, "terminal %d out of range", i);
+    return EMV_OK;
+}
+
+extern "C" int emv_kernel_dev(emv_ctx *c, int32_t n, int64_t arcs, const int32_t *d_row_ptr, const int32_t *d_col,
+                              const int32_t *d_w, int32_t k, const int32_t *terminals, int32_t *d_table, int64_t ld,
+                              int64_t *cost_out, void *stream)
+{
+    if (!c || !d_row_ptr || (arcs > 0 && (!d_col || !d_w)) || !d_table || !cost_out || n <= 0 || arcs < 0 ||
+        arcs >= INT32_MAX || ld < n)
+        return emv_fail(EMV_ERR_BAD_INPUT, "emv_kernel_dev: bad arguments");
+    int r = check_k(n, k, terminals);
+    if (r) return r;
+    CUDA_TRY(cudaSetDevice(c->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    c->launches = 0;
+    r = dev_reserve(c->adj, sizeof(int2) * (size_t)std::max<int64_t>(arcs, 1));
+    if (r) return r;
+    k_pack_adj<<<grid_for(arcs, 256, 4096), 256, 0, st>>>(d_col, d_w, (int2 *)c->adj.ptr, arcs);
+    c->launches++;
+    return run_dp(c, n, d_row_ptr, (const int2 *)c->adj.ptr, k, terminals, d_table, ld, st, cost_out, nullptr);
+}
+
+// Runs the traceback kernel and reduces its edge list to a tree on the host.
+int run_traceback(emv_ctx *c, int32_t n, const int32_t *row_ptr, const int2 *adj, int32_t k, const int32_t *table,
+                  int64_t ld, cudaStream_t st, emv_result *out)
+{
+    const int32_t cap = std::max(64, 2 * n);
+    int r = dev_reserve(c->tb_edges, sizeof(int32_t) * 3 * (size_t)cap);
+    if (!r) r = dev_reserve(c->tb_out, sizeof(int32_t) * 2);
+    if (!r) r = dev_reserve(c->tb_work, sizeof(int32_t) * 3 * (size_t)n);
+    if (r) return r;
+    int32_t *work = (int32_t *)c->tb_work.ptr;
+    CUDA_TRY(cudaMemsetAsync(work + 2 * (size_t)n, 0xff, sizeof(int32_t) * (size_t)n, st));
+    CUDA_TRY(cudaMemsetAsync(c->tb_out.ptr, 0, sizeof(int32_t) * 2, st));
+    TbArgs a;
+    a.table = table;
+    a.ld = ld;
+    a.n = n;
+    a.k = k;
+    a.row_ptr = row_ptr;
+    a.adj = adj;
+    a.terms = (const int32_t *)c->terms.ptr;
+    a.edges = (int32_t *)c->tb_edges.ptr;
+    a.cap = cap;
+    a.out = (int32_t *)c->tb_out.ptr;
+    a.queue = work;
+    a.parent = work + n;
+    a.stamp = work + 2 * (size_t)n;
+    a.max_steps = 4 * n + 64 * k + 1024;
+    CUDA_TRY(cudaEventRecord(c->ev[MAX_EVENTS - 2], st));
+    k_traceback<<<1, 32, 0, st>>>(a);
+    c->launches++;
+    CUDA_TRY(cudaEventRecord(c->ev[MAX_EVENTS - 1], st));
+    int32_t hout[2];
+    CUDA_TRY(cudaMemcpyAsync(hout, a.out, sizeof(hout), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c->ev[MAX_EVENTS - 2], c->ev[MAX_EVENTS - 1]);
+    out->timing.traceback_ms = ms;
+    if (hout[1]) return emv_dev_status_to_emv((uint32_t)hout[1]);
+    std::vector<int32_t> e((size_t)hout[0] * 3);
+    if (hout[0] > 0)
+        CUDA_TRY(cudaMemcpy(e.data(), a.edges, sizeof(int32_t) * e.size(), cudaMemcpyDeviceToHost));
+    // Keep a spanning forest of the emitted edges: duplicates and zero-weight
+    // cycles (possible only through zero-weight arcs) are dropped.
+    std::vector<int32_t> parent((size_t)n);
+    std::iota(parent.begin(), parent.end(), 0);
+    auto find = [&](int32_t x) {
+        while (parent[(size_t)x] != x) {
+            parent[(size_t)x] = parent[(size_t)parent[(size_t)x]];
+            x = parent[(size_t)x];
+        }
+        return x;
+    };
+    int64_t count = 0, weight = 0;
+    for (int32_t i = 0; i < hout[0]; i++) {
+        int32_t u = e[(size_t)3 * i], v = e[(size_t)3 * i + 1], wt = e[(size_t)3 * i + 2];
+        int32_t ru = find(u), rv = find(v);
+        if (ru == rv) continue;
+        parent[(size_t)ru] = rv;
+        if (out->tree && count < out->tree_cap) {
+            out->tree[3 * count] = u;
+            out->tree[3 * count + 1] = v;
+            out->tree[3 * count + 2] = wt;
+        }
+        count++;
+        weight += wt;
+    }
+    out->tree_count = count;
+    out->tree_weight = weight;
+    if (out->tree && count > out->tree_cap)
+        return emv_fail(EMV_ERR_BAD_INPUT, "tree buffer holds %lld edges, need %lld", (long long)out->tree_cap,
+                        (long long)count);
+    return EMV_OK;
+}
+
+int solve_on_device(emv_ctx *c, int32_t n, int64_t arcs, const int32_t *row_ptr, const int32_t *col,
+                    const int32_t *w, const int32_t *terms, int32_t k, int32_t flags, emv_result *out,
+                    cudaStream_t st)
+{
+    int r = dev_reserve(c->adj, sizeof(int2) * (size_t)std::max<int64_t>(arcs, 1));
+    if (r) return r;
+    k_pack_adj<<<grid_for(arcs, 256, 4096), 256, 0, st>>>(col, w, (int2 *)c->adj.ptr, arcs);
+    c->launches++;
+    const int64_t ld = ((int64_t)n + 31) / 32 * 32;
+    const size_t tbytes = sizeof(int32_t) * (size_t)ld << k;
+    r = dev_reserve(c->table, tbytes);
+    if (r) return r;
+    int32_t *table = (int32_t *)c->table.ptr;
+    std::memset(&out->timing, 0, sizeof(out->timing));
+    r = run_dp(c, n, row_ptr, (const int2 *)c->adj.ptr, k, terms, table, ld, st, &out->cost, &out->timing);
+    if (r) return r;
+    out->tree_count = 0;
+    out->tree_weight = 0;
+    if ((flags & EMV_SOLVE_TREE) && k >= 2) {
+        r = run_traceback(c, n, row_ptr, (const int2 *)c->adj.ptr, k, table, ld, st, out);
+        if (r) return r;
+    }
+    if ((flags & EMV_SOLVE_TABLE) && out->table) {
+        CUDA_TRY(cudaMemcpy2DAsync(out->table, sizeof(int32_t) * (size_t)n, table, sizeof(int32_t) * (size_t)ld,
+                                   sizeof(int32_t) * (size_t)n, (size_t)1 << k, cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+    }
+    out->timing.launches = c->launches;
+    return EMV_OK;
+}
+
+extern "C" int emv_solve(emv_ctx *c, const emv_graph *g, const int32_t *terminals, int32_t k, int32_t flags,
+                         emv_result *out, void *stream)
+{
+    if (!c || !out) return emv_fail(EMV_ERR_BAD_INPUT, "null argument");
+    int r = emv_graph_validate(g);
+    if (r) return r;
+    r = check_k(g->n, k, terminals);
+    if (r) return r;
+    if (!(flags & EMV_SOLVE_NOCHECK)) {
+        r = emv_graph_check(g, nullptr);
+        if (r) return r;
+    }
+    CUDA_TRY(cudaSetDevice(c->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    c->launches = 0;
+    const int32_t n = g->n;
+    const int64_t arcs = g->arcs;
+    r = dev_reserve(c->g_row, sizeof(int32_t) * ((size_t)n + 1));
+    if (!r) r = dev_reserve(c->g_col, sizeof(int32_t) * (size_t)std::max<int64_t>(arcs, 1));
+    if (!r) r = dev_reserve(c->g_w, sizeof(int32_t) * (size_t)std::max<int64_t>(arcs, 1));
+    if (r) return r;
+    CUDA_TRY(cudaMemcpyAsync(c->g_row.ptr, g->row_ptr, sizeof(int32_t) * ((size_t)n + 1), cudaMemcpyHostToDevice, st));
+    if (arcs > 0) {
+        CUDA_TRY(cudaMemcpyAsync(c->g_col.ptr, g->col, sizeof(int32_t) * (size_t)arcs, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(c->g_w.ptr, g->w, sizeof(int32_t) * (size_t)arcs, cudaMemcpyHostToDevice, st));
+    }
+    return solve_on_device(c, n, arcs, (const int32_t *)c->g_row.ptr, (const int32_t *)c->g_col.ptr,
+                           (const int32_t *)c->g_w.ptr, terminals, k, flags, out, st);
+}
+
+extern "C" int emv_solve_dev(emv_ctx *c, const emv_graph *d_g, const int32_t *terminals, int32_t k, int32_t flags,
+                             emv_result *out, void *stream)
+{
+    if (!c || !out) return emv_fail(EMV_ERR_BAD_INPUT, "null argument");
+    int r = emv_graph_validate(d_g);
+    if (r) return r;
+    r = check_k(d_g->n, k, terminals);
+    if (r) return r;
+    CUDA_TRY(cudaSetDevice(c->device));
+    c->launches = 0;
+    return solve_on_device(c, d_g->n, d_g->arcs, d_g->row_ptr, d_g->col, d_g->w, terminals, k, flags, out,
+                           (cudaStream_t)stream);
+}
+
+extern "C" int emv_sssp(emv_ctx *c, const emv_graph *g, int32_t source, int64_t *dist_out, float *ms_out, void *stream)
+{
+    if (!c || !dist_out) return emv_fail(EMV_ERR_BAD_INPUT, "null argument");
+    int r = emv_graph_validate(g);
+    if (r) return r;
+    if (source < 0 || source >= g->n) return emv_fail(EMV_ERR_BAD_INPUT, "source out of range");
+    CUDA_TRY(cudaSetDevice(c->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    const int32_t n = g->n;
+    const int64_t arcs = g->arcs;
+    r = dev_reserve(c->g_row, sizeof(int32_t) * ((size_t)n + 1));
+    if (!r) r = dev_reserve(c->g_col, sizeof(int32_t) * (size_t)std::max<int64_t>(arcs, 1));
+    if (!r) r = dev_reserve(c->g_w, sizeof(int32_t) * (size_t)std::max<int64_t>(arcs, 1));
+    if (!r) r = dev_reserve(c->adj, sizeof(int2) * (size_t)std::max<int64_t>(arcs, 1));
+    if (!r) r = dev_reserve(c->table, sizeof(int32_t) * 2 * (size_t)n);  // row 1 = {source}
+    if (!r) r = dev_reserve(c->terms, sizeof(int32_t));
+    if (!r) r = prepare_subsets(c, 1, st);
+    if (!r) r = reserve_relax(c, n);
+    if (r) return r;
+    CUDA_TRY(cudaMemcpyAsync(c->g_row.ptr, g->row_ptr, sizeof(int32_t) * ((size_t)n + 1), cudaMemcpyHostToDevice, st));
+    if (arcs > 0) {
+        CUDA_TRY(cudaMemcpyAsync(c->g_col.ptr, g->col, sizeof(int32_t) * (size_t)arcs, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(c->g_w.ptr, g->w, sizeof(int32_t) * (size_t)arcs, cudaMemcpyHostToDevice, st));
+    }
+    CUDA_TRY(cudaMemcpyAsync(c->terms.ptr, &source, sizeof(int32_t), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemsetAsync(c->stat.ptr, 0, sizeof(DevStat), st));
+    CUDA_TRY(cudaEventRecord(c->ev[0], st));
+    k_pack_adj<<<grid_for(arcs, 256, 4096), 256, 0, st>>>((const int32_t *)c->g_col.ptr, (const int32_t *)c->g_w.ptr,
+                                                          (int2 *)c->adj.ptr, arcs);
+    r = launch_relax(c, (const int32_t *)c->g_row.ptr, (const int2 *)c->adj.ptr, n, n, (int32_t *)c->table.ptr,
+                     (const uint32_t *)c->xs.ptr, 1, (const int32_t *)c->terms.ptr, 1, st);
+    if (r) return r;
+    CUDA_TRY(cudaEventRecord(c->ev[1], st));
+    std::vector<int32_t> d((size_t)n);
+    CUDA_TRY(cudaMemcpyAsync(d.data(), (int32_t *)c->table.ptr + n, sizeof(int32_t) * (size_t)n,
+                             cudaMemcpyDeviceToHost, st));
+    DevStat ds;
+    CUDA_TRY(cudaMemcpyAsync(&ds, c->stat.ptr, sizeof(ds), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    if (ds.err) return emv_dev_status_to_emv(ds.err);
+    if (ms_out) cudaEventElapsedTime(ms_out, c->ev[0], c->ev[1]);
+    for (int32_t v = 0; v < n; v++) dist_out[v] = d[(size_t)v] >= INF ? INT64_MAX : (int64_t)d[(size_t)v];
+    return EMV_OK;
+}

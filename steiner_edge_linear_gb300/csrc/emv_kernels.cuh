@@ -1,0 +1,444 @@
+// emv_kernels.cuh -- sm_103a kernels of the EMV dynamic program.
+//
+// Table: int32 d[X * ld + v], subset-major like the reference's FV_INDEX
+// (reader/reader-el.c:691), EMV_INF32 = 2^30 for "no value".  All finite
+// values are below 2^30 (checked on the host), so a + b of two table values
+// fits in uint32 and a value + an arc weight fits in int32.
+//
+// Kernels (reference step each one replaces):
+//   k_fill        f_v = INF                          R:2243-2259
+//   k_pack_adj    (col, w) arcs packed as int2        R:794-826 (adjacency fill)
+//   k_merge       subset merge of one level           R:2068-2107
+//   k_relax_chunk multi-source closure of <= 32 rows  R:2109-2130, R:1762-1880
+//                 (also the k level-1 SSSPs,          R:1988-2031)
+//   k_traceback   tree recovery by recomputation      R:1907-1944
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "emv_common.cuh"
+
+namespace emv {
+
+struct RelaxArgs {
+    const int32_t *row_ptr;
+    const int2 *adj;
+    int32_t n;
+    int64_t ld;
+    int32_t *table;
+    const uint32_t *rows;   // subsets of this chunk
+    int32_t nrows;          // <= CHUNK_ROWS
+    const int32_t *terms;   // level-1 mode: row r is {r}, source terms[r]
+    int32_t level1;
+    int32_t *scratch;       // vertex-major chunk buffer, n * CHUNK_ROWS int32
+    uint8_t *act0;          // active flags, n bytes each
+    uint8_t *act1;
+    uint32_t *ctrl;         // C_WORDS words
+    DevStat *stat;
+    int32_t max_sweeps;
+};
+
+// Grid-wide barrier for a cooperative launch.  Bounded: a block that waits
+// longer than SPIN_LIMIT iterations, or sees another block's error, records
+// the error and returns false; every block then leaves the kernel.
+__device__ __forceinline__ bool grid_barrier(uint32_t *ctrl, int *s_ok)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile uint32_t *vc = ctrl;
+        const uint32_t gen = vc[C_BAR_GEN];
+        __threadfence();
+        const uint32_t arrived = atomicAdd(ctrl + C_BAR_COUNT, 1u);
+        if (arrived == gridDim.x - 1) {
+            atomicExch(ctrl + C_BAR_COUNT, 0u);
+            __threadfence();
+            atomicAdd(ctrl + C_BAR_GEN, 1u);
+        } else {
+            uint32_t spins = 0;
+            while (vc[C_BAR_GEN] == gen) {
+                if (vc[C_ERR] != 0) break;
+                if (++spins > SPIN_LIMIT) {
+                    atomicOr(ctrl + C_ERR, (uint32_t)EMV_DEV_BARRIER_TIMEOUT);
+                    break;
+                }
+                __nanosleep(256);
+            }
+        }
+        __threadfence();
+        *s_ok = (vc[C_ERR] == 0);
+    }
+    __syncthreads();
+    return *s_ok != 0;
+}
+
+__global__ void k_fill(int32_t *__restrict__ p, int64_t count, int32_t value)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (; i < count; i += stride) p[i] = value;
+}
+
+__global__ void k_pack_adj(const int32_t *__restrict__ col, const int32_t *__restrict__ w,
+                           int2 *__restrict__ adj, int64_t arcs)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (; i < arcs; i += stride) adj[i] = make_int2(col[i], w[i]);
+}
+
+// Subset merge of one level m (R:2068-2088) plus the terminal override of
+// the virtual-source arcs (R:2099-2107).  Block (vertex block of 32, group
+// of subsets); a warp takes one subset X at a time and its lanes 32 vertices.
+// The unordered pairs {Y, X\Y} are enumerated once each (Y holds the lowest
+// terminal of X); min is order-independent, so the values equal the
+// reference's ordered-pair loop.  Lower-level rows are read-only here.
+__global__ void __launch_bounds__(256) k_merge(int32_t *__restrict__ table, int64_t ld, int32_t n,
+                                               const uint32_t *__restrict__ xs, int32_t cnt, int32_t xper,
+                                               const int32_t *__restrict__ terms, int32_t k)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int32_t v = blockIdx.x * 32 + lane;
+    const int32_t xb = blockIdx.y * xper, xe = min(cnt, xb + xper);
+    if (v >= n) return;
+    for (int32_t xi = xb + warp; xi < xe; xi += nw) {
+        const uint32_t X = __ldg(xs + xi);
+        const uint32_t low = X & (0u - X), rest = X ^ low;
+        uint32_t acc = (uint32_t)INF;
+        uint32_t s = 0;
+        do {
+            const uint32_t Y = low | s, Z = X ^ Y;
+            const uint32_t a = (uint32_t)__ldg(table + (int64_t)Y * ld + v);
+            const uint32_t b = (uint32_t)__ldg(table + (int64_t)Z * ld + v);
+            acc = min(acc, a + b);
+            s = (s - rest) & rest;
+        } while (s != rest);
+        for (uint32_t bits = X; bits; bits &= bits - 1) {
+            const int t = __ffs(bits) - 1;
+            if (__ldg(terms + t) == v) acc = (uint32_t)__ldg(table + (int64_t)(X ^ (1u << t)) * ld + v);
+        }
+        table[(int64_t)X * ld + v] = (int32_t)acc;
+    }
+}
+
+// Multi-source shortest-path closure of up to 32 rows (R:2109-2130): for
+// every row X of the chunk, d[X][v] = min over u of init[u] + dist(u, v).
+// One cooperative persistent launch:
+//   A. transpose the rows into a vertex-major buffer (vertex v: 32 ints, one
+//      128-byte line) -- in level-1 mode the rows are k single-source inits;
+//   B. frontier sweeps: a warp owns a vertex, lane r its row r; it pulls
+//      min over arcs (u, w) of d[u] + w with coalesced 128-byte gathers and
+//      writes in place (only the owner writes, values only decrease, so no
+//      atomics are needed); a vertex that decreased marks its neighbours
+//      active for the next sweep; sweeps end when one changes nothing
+//      (bounded by n + 1 sweeps, the Bellman-Ford bound);
+//   C. transpose back into the table rows.
+// Scratch reads use ld.global.cg (L2, never a stale L1 line).
+__global__ void __launch_bounds__(RELAX_THREADS) k_relax_chunk(RelaxArgs a)
+{
+    __shared__ int32_t tile[32][33];
+    __shared__ int s_ok;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwb = blockDim.x >> 5;
+    const int32_t n = a.n;
+    const int32_t ntiles = (n + 31) >> 5;
+    const int32_t nrows = a.nrows;
+
+    // ---- A: rows -> vertex-major buffer
+    for (int32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const int32_t v = t * 32 + lane;
+        for (int r = warp; r < 32; r += nwb) {
+            int32_t x = INF;
+            if (r < nrows && v < n) {
+                if (a.level1) x = (v == __ldg(a.terms + r)) ? 0 : INF;
+                else x = __ldcg(a.table + (int64_t)__ldg(a.rows + r) * a.ld + v);
+            }
+            tile[r][lane] = x;
+        }
+        __syncthreads();
+        for (int vv = warp; vv < 32; vv += nwb) {
+            const int32_t v2 = t * 32 + vv;
+            if (v2 < n) __stcg(a.scratch + (int64_t)v2 * 32 + lane, tile[lane][vv]);
+        }
+        __syncthreads();
+    }
+    for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        a.act0[v] = 1;
+        a.act1[v] = 0;
+    }
+    if (!grid_barrier(a.ctrl, &s_ok)) return;
+
+    // ---- B: frontier sweeps
+    const int32_t gw = (int32_t)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int32_t nwg = (int32_t)((gridDim.x * blockDim.x) >> 5);
+    volatile uint32_t *vctrl = a.ctrl;
+    int32_t s = 0;
+    bool converged = false;
+    for (; s < a.max_sweeps; s++) {
+        uint8_t *cur = (s & 1) ? a.act1 : a.act0;
+        uint8_t *nxt = (s & 1) ? a.act0 : a.act1;
+        if (blockIdx.x == 0 && threadIdx.x == 0) vctrl[C_SLOT0 + (s + 1) % 3] = 0;
+        bool any = false;
+        for (int32_t v = gw; v < n; v += nwg) {
+            if (__ldcg(cur + v) == 0) continue;
+            if (lane == 0) cur[v] = 0;
+            const int32_t beg = __ldg(a.row_ptr + v), end = __ldg(a.row_ptr + v + 1);
+            int32_t *sv = a.scratch + (int64_t)v * 32 + lane;
+            const int32_t old = __ldcg(sv);
+            int32_t acc = old;
+            for (int32_t e0 = beg; e0 < end; e0 += 32) {
+                const int32_t e = e0 + lane;
+                int2 arc = make_int2(0, 0);
+                if (e < end) arc = __ldg(a.adj + e);
+                const int cntj = min(32, end - e0);
+#pragma unroll 4
+                for (int j = 0; j < cntj; j++) {
+                    const int32_t u = __shfl_sync(FULL, arc.x, j);
+                    const int32_t wt = __shfl_sync(FULL, arc.y, j);
+                    acc = min(acc, __ldcg(a.scratch + (int64_t)u * 32 + lane) + wt);
+                }
+            }
+            const bool dec = acc < old;
+            if (dec) __stcg(sv, acc);
+            if (__ballot_sync(FULL, dec)) {
+                any = true;
+                for (int32_t e = beg + lane; e < end; e += 32) nxt[__ldg(&a.adj[e].x)] = 1;
+            }
+        }
+        any = __syncthreads_or(any);
+        if (any && threadIdx.x == 0) vctrl[C_SLOT0 + s % 3] = 1;
+        if (!grid_barrier(a.ctrl, &s_ok)) return;
+        if (vctrl[C_SLOT0 + s % 3] == 0) {
+            converged = true;
+            s++;
+            break;
+        }
+    }
+    if (!converged) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&a.stat->err, (uint32_t)EMV_DEV_SWEEP_LIMIT);
+        return;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.stat->sweeps, (unsigned long long)s);
+
+    // ---- C: vertex-major buffer -> rows
+    for (int32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        for (int vv = warp; vv < 32; vv += nwb) {
+            const int32_t v2 = t * 32 + vv;
+            tile[vv][lane] = (v2 < n) ? __ldcg(a.scratch + (int64_t)v2 * 32 + lane) : INF;
+        }
+        __syncthreads();
+        const int32_t v = t * 32 + lane;
+        if (v < n)
+            for (int r = warp; r < nrows; r += nwb) a.table[(int64_t)__ldg(a.rows + r) * a.ld + v] = tile[lane][r];
+        __syncthreads();
+    }
+}
+
+// Records a launch-level barrier error into the solve status.
+__global__ void k_collect_err(const uint32_t *ctrl, DevStat *stat)
+{
+    if (threadIdx.x == 0 && ctrl[C_ERR] != 0) atomicOr(&stat->err, ctrl[C_ERR]);
+}
+
+// ------------------------------------------------------------- traceback
+
+__device__ __forceinline__ uint32_t deposit_bits(uint32_t p, uint32_t mask)
+{
+    uint32_t r = 0;
+    for (uint32_t b = 1; mask; b <<= 1) {
+        const uint32_t lowbit = mask & (0u - mask);
+        if (p & b) r |= lowbit;
+        mask ^= lowbit;
+    }
+    return r;
+}
+
+struct TbArgs {
+    const int32_t *table;
+    int64_t ld;
+    int32_t n;
+    int32_t k;
+    const int32_t *row_ptr;
+    const int2 *adj;
+    const int32_t *terms;
+    int32_t *edges;     // 3 * cap
+    int32_t cap;
+    int32_t *out;       // [0] edge count, [1] status
+    int32_t *queue;     // n
+    int32_t *parent;    // n
+    int32_t *stamp;     // n, -1 on entry
+    int32_t max_steps;
+};
+
+// Witness of d[X][v] (warp-collective, all lanes return the same):
+// 0 leaf (X = {i}, v = t_i); 1 split d[Y][v] + d[X\Y][v] = D (the lowest
+// pair index); 2 arc (u, v) of positive weight with d[X][u] + w = D;
+// 3 none of those (a zero-weight predecessor must exist).
+__device__ int tb_witness(const TbArgs &a, uint32_t X, int32_t v, int32_t D, uint32_t &Y, int32_t &u, int32_t &wt)
+{
+    const int lane = threadIdx.x & 31;
+    const int pc = __popc(X);
+    if (pc == 1 && v == __ldg(a.terms + (__ffs(X) - 1))) return 0;
+    if (pc >= 2) {
+        const uint32_t low = X & (0u - X), rest = X ^ low;
+        const uint32_t npairs = (1u << __popc(rest)) - 1;
+        for (uint32_t base = 0; base < npairs; base += 32) {
+            const uint32_t p = base + lane;
+            bool ok = false;
+            uint32_t y = 0;
+            if (p < npairs) {
+                y = low | deposit_bits(p, rest);
+                const int32_t x1 = a.table[(int64_t)y * a.ld + v];
+                const int32_t x2 = a.table[(int64_t)(X ^ y) * a.ld + v];
+                ok = x1 < INF && x2 < INF && x1 + x2 == D;
+            }
+            const unsigned bal = __ballot_sync(FULL, ok);
+            if (bal) {
+                Y = __shfl_sync(FULL, y, __ffs(bal) - 1);
+                return 1;
+            }
+        }
+    }
+    const int32_t beg = a.row_ptr[v], end = a.row_ptr[v + 1];
+    for (int32_t e0 = beg; e0 < end; e0 += 32) {
+        const int32_t e = e0 + lane;
+        bool ok = false;
+        int2 arc = make_int2(0, 0);
+        if (e < end) {
+            arc = a.adj[e];
+            if (arc.y > 0) {
+                const int32_t du = a.table[(int64_t)X * a.ld + arc.x];
+                ok = du < INF && du + arc.y == D;
+            }
+        }
+        const unsigned bal = __ballot_sync(FULL, ok);
+        if (bal) {
+            const int src = __ffs(bal) - 1;
+            u = __shfl_sync(FULL, arc.x, src);
+            wt = __shfl_sync(FULL, arc.y, src);
+            return 2;
+        }
+    }
+    return 3;
+}
+
+// Tree recovery from the finished table (one warp).  Starts at (C, q) and
+// repeatedly explains d[X][v] by a leaf, a split into (Y, v) and (X\Y, v),
+// or an arc (v, u) into (X, u) -- the decisions the reference records in b_v
+// (R:2081-2084, R:2122-2128) and walks in backtrack() (R:1907-1932), found
+// here by recomputation instead of a 2x-table predecessor store.  A run of
+// zero-weight arcs is resolved by a breadth-first search inside the set of
+// vertices with the same value, so zero-weight cycles cannot loop.
+__global__ void __launch_bounds__(32) k_traceback(TbArgs a)
+{
+    __shared__ uint32_t stX[TB_STACK];
+    __shared__ int32_t stV[TB_STACK];
+    const int lane = threadIdx.x & 31;
+    int sp = 0, cnt = 0, walk = 0, steps = 0;
+    uint32_t status = 0;
+    if (a.k >= 2) {
+        if (lane == 0) {
+            stX[0] = (1u << (a.k - 1)) - 1;
+            stV[0] = a.terms[a.k - 1];
+        }
+        sp = 1;
+    }
+    __syncwarp();
+    while (sp > 0) {
+        if (++steps > a.max_steps) { status |= EMV_DEV_TB_STEPS; break; }
+        const uint32_t X = stX[sp - 1];
+        const int32_t v = stV[sp - 1];
+        sp--;
+        __syncwarp();
+        const int32_t D = a.table[(int64_t)X * a.ld + v];
+        uint32_t Y = 0;
+        int32_t u = 0, wt = 0;
+        const int kind = tb_witness(a, X, v, D, Y, u, wt);
+        if (kind == 0) continue;
+        if (kind == 1) {
+            if (sp + 2 > TB_STACK) { status |= EMV_DEV_TB_OVERFLOW; break; }
+            if (lane == 0) {
+                stX[sp] = Y; stV[sp] = v;
+                stX[sp + 1] = X ^ Y; stV[sp + 1] = v;
+            }
+            sp += 2;
+            __syncwarp();
+            continue;
+        }
+        if (kind == 2) {
+            if (cnt >= a.cap || sp + 1 > TB_STACK) { status |= EMV_DEV_TB_OVERFLOW; break; }
+            if (lane == 0) {
+                a.edges[3 * cnt] = v; a.edges[3 * cnt + 1] = u; a.edges[3 * cnt + 2] = wt;
+                stX[sp] = X; stV[sp] = u;
+            }
+            cnt++;
+            sp++;
+            __syncwarp();
+            continue;
+        }
+        // Zero-weight run: BFS over arcs of weight 0 between vertices of value D.
+        walk++;
+        if (lane == 0) {
+            a.queue[0] = v;
+            a.parent[v] = -1;
+            a.stamp[v] = walk;
+        }
+        __syncwarp();
+        int32_t head = 0, tail = 1, target = -1;
+        while (head < tail) {
+            const int32_t x = *(volatile int32_t *)(a.queue + head);
+            head++;
+            if (x != v) {
+                uint32_t Y2;
+                int32_t u2, w2;
+                if (tb_witness(a, X, x, D, Y2, u2, w2) != 3) { target = x; break; }
+            }
+            const int32_t beg = a.row_ptr[x], end = a.row_ptr[x + 1];
+            for (int32_t e0 = beg; e0 < end; e0 += 32) {
+                const int32_t e = e0 + lane;
+                bool add = false;
+                int32_t y = 0;
+                if (e < end) {
+                    const int2 arc = a.adj[e];
+                    y = arc.x;
+                    if (arc.y == 0 && a.table[(int64_t)X * a.ld + y] == D)
+                        add = atomicExch(a.stamp + y, walk) != walk;
+                }
+                const unsigned bal = __ballot_sync(FULL, add);
+                if (add) {
+                    const int pos = tail + __popc(bal & ((1u << lane) - 1));
+                    a.queue[pos] = y;
+                    a.parent[y] = x;
+                }
+                tail += __popc(bal);
+                __syncwarp();
+            }
+        }
+        if (target < 0) { status |= EMV_DEV_TB_NO_WITNESS; break; }
+        int32_t z = target, emitted = 0;
+        bool ovf = false;
+        if (lane == 0) {
+            while (z != v) {
+                const int32_t p = *(volatile int32_t *)(a.parent + z);
+                if (cnt + emitted >= a.cap) { ovf = true; break; }
+                a.edges[3 * (cnt + emitted)] = z;
+                a.edges[3 * (cnt + emitted) + 1] = p;
+                a.edges[3 * (cnt + emitted) + 2] = 0;
+                emitted++;
+                z = p;
+            }
+        }
+        emitted = __shfl_sync(FULL, emitted, 0);
+        ovf = __shfl_sync(FULL, (int)ovf, 0) != 0;
+        cnt += emitted;
+        if (ovf || sp + 1 > TB_STACK) { status |= EMV_DEV_TB_OVERFLOW; break; }
+        if (lane == 0) { stX[sp] = X; stV[sp] = target; }
+        sp++;
+        __syncwarp();
+    }
+    if (lane == 0) {
+        a.out[0] = cnt;
+        a.out[1] = (int32_t)status;
+    }
+}
+
+}  // namespace emv

@@ -1,0 +1,63 @@
+// emv_solver.h -- the solver context and the host-side helpers of the GPU DP.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+#include "emv_internal.h"
+
+#define CUDA_TRY(x)                                                                                        \
+    do {                                                                                                   \
+        cudaError_t e_ = (x);                                                                              \
+        if (e_ != cudaSuccess) {                                                                           \
+            cudaGetLastError();                                                                            \
+            return emv_fail(EMV_ERR_CUDA, "%s: %s (%s:%d)", #x, cudaGetErrorString(e_), __FILE__, __LINE__); \
+        }                                                                                                  \
+    } while (0)
+
+// A device allocation that only grows (freed on context destruction).
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+};
+
+int dev_reserve(DevBuf &b, size_t bytes);
+void dev_release(DevBuf &b);
+
+constexpr int MAX_EVENTS = 64;
+constexpr int BATCH_CLASSES = 12;  // (n bucket 0..3) x (k bucket 0..2)
+
+struct emv_ctx {
+    int device = 0;
+    int sms = 0;
+    int relax_blocks_max = 0;
+    DevBuf ctrl, stat;             // relaxation barrier words, solve status
+    DevBuf scratch, act;           // vertex-major chunk buffer, active flags
+    DevBuf adj;                    // packed (col, w) arcs
+    DevBuf xs, terms;              // subsets by level, terminals
+    DevBuf g_row, g_col, g_w;      // device copy of a host CSR
+    DevBuf table;                  // DP table of emv_solve
+    DevBuf tb_edges, tb_out, tb_work;
+    void *pinned = nullptr;        // small pinned host buffer for scalar reads
+    cudaEvent_t ev[MAX_EVENTS] = {};
+    int32_t xs_k = -1;             // k of the cached subset list
+    std::vector<uint32_t> xs_host;
+    std::vector<int64_t> xs_off;   // level m occupies xs[off[m], off[m+1])
+    int64_t launches = 0;
+    // batched launch
+    DevBuf bxs, bxs_off;           // subset lists of every k <= BATCH_KMAX
+    bool bxs_ready = false;
+    int batch_blocks = 0;
+    DevBuf b_row, b_adj, b_term, b_desc, b_table, b_costs, b_ctrl;
+    void *bstage = nullptr;        // pinned staging of the packed batch
+    size_t bstage_bytes = 0;
+    cudaGraphExec_t bgraph_exec = nullptr;
+    char bgraph_args[160] = {};    // BatchArgs of the captured graph
+    int32_t tune_rcap[BATCH_CLASSES] = {};
+};
+
+void subset_levels(int32_t k, std::vector<uint32_t> &xs, std::vector<int64_t> &off);
+int prepare_subsets(emv_ctx *c, int32_t k, cudaStream_t st);
+int reserve_relax(emv_ctx *c, int32_t n);

@@ -1,0 +1,174 @@
+"""GPU parity: the sm_103a solver against the oracle and the reference's golden tables.
+
+The bar is bit-exact: the whole int32 DP table and the cost equal the
+oracle's on the same instance and the reference's golden hashes; the tree is a
+valid Steiner tree of real edges whose weight equals the cost.
+"""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from tests.golden.cases import CASES, instance_for, instance_fnv
+from tests.helpers import check_tree, table_row_fnv
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def solver(emv):
+    s = emv.Solver(0)
+    yield s
+    s.close()
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_table_and_cost_match_oracle_and_golden(name, emv, orc, golden, solver):
+    g = golden["cases"][name]
+    inst = instance_for(CASES[name])
+    assert instance_fnv(inst) == g["instance_fnv"]
+    csr = emv.Csr.from_stp(inst)
+    res = solver.solve(csr, tree=True, table=True)
+    want, want_cost = orc.emv_table(csr.n, csr.row_ptr, csr.col, csr.w, csr.terminals, threads=8)
+    assert res.cost == want_cost == g["cost"]
+    mism = np.argwhere(res.table != want)
+    assert mism.size == 0, f"{len(mism)} cells differ, first (X, v) = {mism[:5].tolist()}"
+    assert f"{orc.fnv64(res.table):016x}" == g["table_fnv"]
+    if "row_fnv" in g and csr.k <= 8:
+        assert table_row_fnv(res.table) == g["row_fnv"]
+    check_tree(csr.n, inst.edges, res.tree, csr.terminals, res.cost)
+    assert res.tree_weight == res.cost or csr.k == 1
+
+
+def test_repeat_solves_identical(emv, solver):
+    inst = emv.StpInstance.regular(5000, 6, 1, 1000, 9, 77)
+    csr = emv.Csr.from_stp(inst)
+    a = solver.solve(csr, table=True)
+    b = solver.solve(csr, table=True)
+    assert a.cost == b.cost and np.array_equal(a.table, b.table)
+
+
+def test_kernel_dev_on_caller_table(emv, orc, solver):
+    torch = pytest.importorskip("torch")
+    inst = emv.StpInstance.regular(3000, 8, 1, 1000, 7, 31337)
+    csr = emv.Csr.from_stp(inst)
+    dev = torch.device("cuda:0")
+    row = torch.from_numpy(csr.row_ptr).to(dev)
+    col = torch.from_numpy(csr.col).to(dev)
+    w = torch.from_numpy(csr.w).to(dev)
+    ld = csr.n + 5  # any stride >= n
+    table = torch.full(((1 << csr.k), ld), -7, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream().cuda_stream
+    cost = solver.kernel_dev(csr.n, csr.arcs, row.data_ptr(), col.data_ptr(), w.data_ptr(), csr.terminals,
+                             table.data_ptr(), ld, stream)
+    torch.cuda.synchronize()
+    want, want_cost = orc.emv_table(csr.n, csr.row_ptr, csr.col, csr.w, csr.terminals, threads=8)
+    got = table[:, :csr.n].cpu().numpy()
+    assert cost == want_cost
+    assert np.array_equal(got, want)
+    assert (table[:, csr.n:].cpu().numpy() == -7).all(), "padding columns must stay untouched"
+
+
+def test_solve_dev_matches_solve(emv, solver):
+    torch = pytest.importorskip("torch")
+    inst = emv.StpInstance.regular(2500, 4, 1, 100, 8, 5)
+    csr = emv.Csr.from_stp(inst)
+    dev = torch.device("cuda:0")
+    row, col, w = (torch.from_numpy(a).to(dev) for a in (csr.row_ptr, csr.col, csr.w))
+    torch.cuda.synchronize()
+    r1 = solver.solve_dev(csr.n, csr.arcs, row.data_ptr(), col.data_ptr(), w.data_ptr(), csr.terminals, tree=True)
+    r2 = solver.solve(csr)
+    assert r1.cost == r2.cost
+    check_tree(csr.n, inst.edges, r1.tree, csr.terminals, r1.cost)
+
+
+def test_sssp_matches_oracle(emv, orc, solver):
+    inst = emv.StpInstance.regular(20000, 6, 1, 1000, 2, 8)
+    csr = emv.Csr.from_stp(inst)
+    for s in (0, 12345, 19999):
+        d, _ = solver.sssp(csr, s)
+        assert np.array_equal(d, orc.sssp(csr.n, csr.row_ptr, csr.col, csr.w, s))
+
+
+def test_large_single_solve_properties(emv, orc, solver):
+    """n = 1e5, degree 20, k = 12 (the single large solve): the full table is
+    too slow for the oracle here, so check it through size-independent
+    properties plus exact rows over the first 5 terminals (d[X][v] depends on
+    the terminals of X only; the oracle computes those 32 rows)."""
+    inst = emv.StpInstance.regular(100000, 20, 1, 100, 12, 123456789)
+    csr = emv.Csr.from_stp(inst)
+    res = solver.solve(csr, tree=True, table=True)
+    t = res.table
+    sub, _ = orc.emv_table(csr.n, csr.row_ptr, csr.col, csr.w, csr.terminals[:5], threads=16)
+    assert np.array_equal(t[:32], sub)
+    assert (t[0] == emv.INF32).all() and (t[1:] < emv.INF32).all()
+    rng = np.random.default_rng(0)
+    src = np.repeat(np.arange(csr.n), np.diff(csr.row_ptr))
+    for X in rng.integers(1, 1 << 12, size=24):
+        row = t[X]
+        # closure: d[X][v] <= d[X][u] + w(u, v) for every arc
+        assert (row[csr.col] <= row[src] + csr.w).all()
+        # monotone in X and bounded by every split
+        for b in range(12):
+            if X >> b & 1:
+                assert (t[X ^ (1 << b)] <= row).all()
+                Y = X & ~(1 << b)
+                if Y:
+                    assert (row <= t[Y] + t[1 << b]).all()
+    assert res.cost == int(t[(1 << 11) - 1, csr.terminals[11]])
+    check_tree(csr.n, inst.edges, res.tree, csr.terminals, res.cost)
+
+
+def test_bad_inputs_report_status(emv, solver):
+    disc = emv.StpInstance.from_text(
+        "section graph\nnodes 4\nedges 2\ne 1 2 3\ne 3 4 5\nend\nsection terminals\nterminals 2\nt 1\nt 3\nend\n")
+    csr = emv.Csr.from_stp(disc)
+    with pytest.raises(emv.EmvError) as ei:
+        solver.solve(csr)
+    assert ei.value.status == 7  # EMV_ERR_DISCONNECTED
+    inst = emv.StpInstance.regular(100, 4, 1, 10, 5, 1)
+    csr = emv.Csr.from_stp(inst)
+    with pytest.raises(emv.EmvError) as ei:
+        solver.solve(csr, terminals=[0, 1, 200])
+    assert ei.value.status == 1
+    with pytest.raises(emv.EmvError):
+        solver.solve(csr, terminals=list(range(21)))
+    # the context stays usable after errors
+    assert solver.solve(csr).cost > 0
+
+
+def test_cli_reference_lines(emv, tmp_path):
+    """reader-el-gpu -el -list prints the reference's lines; the regexes are
+    those of the reference's scripts (experiments/verify.py:126-147)."""
+    import re
+
+    inst = emv.StpInstance.regular(3000, 4, 1, 1000, 9, 2718)
+    csr = emv.Csr.from_stp(inst)
+    cost = emv.Solver().solve(csr).cost
+    inst.cost = cost
+    path = str(tmp_path / "i.stp")
+    inst.write(path)
+    out = subprocess.run([emv.CLI_PATH, "-in", path, "-el", "-list"], stdout=subprocess.PIPE, text=True,
+                         check=True).stdout
+    line = next(ln for ln in out.splitlines() if ln.startswith("erickson"))
+    mt = re.search(r"erickson: \[zero:(.*)ms\] \[kernel:(.*)ms (.*)GiB/s\] \[traceback: (.*)ms\] done. "
+                   r"\[(.*)ms\] \[cost:(.*)] {peak:(.*)GiB} {curr:(.*)GiB}", line)
+    assert mt and int(mt.group(6)) == cost
+    inp = next(ln for ln in out.splitlines() if ln.startswith("input"))
+    assert re.search(r"(.*)n = (.*), m = (.*), k = (.*), cost = (.*) \[(.*)ms\] {peak:(.*)GiB} {curr:(.*)GiB}", inp)
+    sol = next(ln for ln in out.splitlines() if ln.startswith("solution"))
+    pairs = re.findall(r'"([^"]*)"', sol)
+    lookup = {}
+    for u, v, w in inst.edges:
+        lookup.setdefault((min(u, v), max(u, v)), set()).add(int(w))
+    tree = []
+    for p in pairs:
+        u, v = (int(x) - 1 for x in p.split())
+        tree.append((u, v, min(lookup[(min(u, v), max(u, v))])))
+    check_tree(inst.n, inst.edges, np.array(tree), inst.terminals, cost)
+    # a wrong cost line in the input ends the run with ERROR, as in the reference
+    inst.cost = cost + 1
+    inst.write(path)
+    r = subprocess.run([emv.CLI_PATH, "-in", path, "-el"], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
+    assert r.returncode != 0 and "min_cost != cost" in r.stderr

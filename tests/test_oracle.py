@@ -1,0 +1,102 @@
+"""The oracle pinned against the reference (CPU only).
+
+* every golden case: the C restatement's table equals the reference's
+  (whole-table and per-row FNV, cost) -- the golden fixtures were written by
+  the reference's own emv_kernel (tests/golden/make_golden.py);
+* the shipped test instances of the reference (testset/, read in place where
+  the reference tree exists): the restatement's cost equals each file's
+  "cost" line, the check the reference itself enforces (reader-el.c:2489-2491),
+  and its whole table equals the reference harness' table;
+* single-source distances against scipy's Dijkstra.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from tests.golden.cases import CASES, instance_for, instance_fnv
+from tests.helpers import table_row_fnv
+
+REF_TESTSET = "/root/reference/testset"
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_oracle_equals_reference_golden(name, emv, orc, golden):
+    g = golden["cases"][name]
+    inst = instance_for(CASES[name])
+    assert instance_fnv(inst) == g["instance_fnv"], "generator drifted from the golden instance"
+    csr = emv.Csr.from_stp(inst)
+    table, cost = orc.emv_table(csr.n, csr.row_ptr, csr.col, csr.w, csr.terminals, threads=4)
+    assert cost == g["cost"]
+    assert f"{orc.fnv64(table):016x}" == g["table_fnv"]
+    if "row_fnv" in g:
+        assert table_row_fnv(table) == g["row_fnv"]
+
+
+def _steinlib_files():
+    files = sorted(glob.glob(os.path.join(REF_TESTSET, "small-instances", "*", "*.stp")))
+    files += sorted(glob.glob(os.path.join(REF_TESTSET, "path", "*.stp")))
+    return files
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_TESTSET), reason="reference test instances not present")
+def test_oracle_costs_on_reference_testset(emv, orc):
+    """All shipped instances: restated cost == the file's cost line; small ones: whole table == reference."""
+    files = _steinlib_files()
+    assert len(files) == 207
+    full_table_checked = 0
+    for f in files:
+        g = emv.graph_load(f)
+        c = emv.root_build(g)
+        if g.k >= 12 and g.n > 200:
+            continue  # covered by the slow test below
+        table, cost = orc.emv_table(c.n, c.row_ptr, c.col, c.w, c.terminals, threads=8)
+        assert cost == g.cost, f
+        if orc.reference_available() and g.k <= 8 and g.n <= 1000:
+            r = orc.ref_emv(f, threads=4)
+            assert r["cost"] == cost and r["fnv"] == orc.fnv64(table), f
+            full_table_checked += 1
+    if orc.reference_available():
+        assert full_table_checked > 60
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_TESTSET), reason="reference test instances not present")
+@pytest.mark.skipif(os.environ.get("EMV_SLOW_TESTS") != "1", reason="set EMV_SLOW_TESTS=1")
+def test_oracle_costs_on_reference_testset_large_k(emv, orc):
+    for f in _steinlib_files():
+        g = emv.graph_load(f)
+        if not (g.k >= 12 and g.n > 200):
+            continue
+        c = emv.root_build(g)
+        _, cost = orc.emv_table(c.n, c.row_ptr, c.col, c.w, c.terminals, threads=8)
+        assert cost == g.cost, f
+
+
+def test_oracle_sssp_matches_scipy(emv, orc):
+    sp = pytest.importorskip("scipy.sparse")
+    csgraph = pytest.importorskip("scipy.sparse.csgraph")
+    inst = emv.StpInstance.regular(3000, 6, 1, 1000, 3, 99)
+    c = emv.Csr.from_stp(inst)
+    rows = np.repeat(np.arange(c.n), np.diff(c.row_ptr))
+    # parallel arcs: keep the lightest one, as a shortest path would
+    lightest = {}
+    for u, v, w in zip(rows.tolist(), c.col.tolist(), c.w.tolist()):
+        if (u, v) not in lightest or w < lightest[(u, v)]:
+            lightest[(u, v)] = w
+    keys = np.array(list(lightest.keys()))
+    vals = np.array(list(lightest.values()), dtype=np.float64)
+    mat = sp.csr_matrix((vals, (keys[:, 0], keys[:, 1])), shape=(c.n, c.n))
+    for s in (0, 17, 2999):
+        ref = csgraph.dijkstra(mat, indices=s)
+        got = orc.sssp(c.n, c.row_ptr, c.col, c.w, s)
+        assert np.array_equal(got, ref.astype(np.int64))
+
+
+def test_oracle_sub_terminal_rows(emv, orc):
+    """d[X][v] depends only on the terminals in X: rows over the first k' terminals agree."""
+    inst = emv.StpInstance.regular(700, 4, 1, 500, 8, 4242)
+    c = emv.Csr.from_stp(inst)
+    full, _ = orc.emv_table(c.n, c.row_ptr, c.col, c.w, c.terminals, threads=4)
+    part, _ = orc.emv_table(c.n, c.row_ptr, c.col, c.w, c.terminals[:5], threads=4)
+    assert np.array_equal(full[:32], part)
