@@ -200,6 +200,17 @@ typedef struct emv_batch_stats {
 int emv_batch_solve(emv_ctx *ctx, const emv_instance *inst, int32_t count,
                     int64_t *costs_out, emv_batch_stats *stats, void *stream);
 
+/* Autotuner of the batched launch (no counterpart in the reference): for
+ * every instance class present in inst (n bucket <=256, <=1024, <=4096,
+ * larger  x  k bucket <=6, 7-8, 9-10: EMV_BATCH_CLASSES classes), times the
+ * relaxation's rows-per-chunk candidates 4, 8, 16, 32 on a sample of that
+ * class and keeps the fastest in the context; rcap_out (may be NULL) gets
+ * EMV_BATCH_CLASSES entries (0 = class not present). */
+#define EMV_BATCH_CLASSES 12
+int emv_batch_autotune(emv_ctx *ctx, const emv_instance *inst, int32_t count, int32_t *rcap_out, void *stream);
+/* Installs a previously tuned table (EMV_BATCH_CLASSES entries, 0 = default). */
+int emv_batch_set_tuning(emv_ctx *ctx, const int32_t *rcap, int32_t classes);
+
 /* -------------------------------------------------------------- serving */
 
 typedef struct emv_server emv_server;

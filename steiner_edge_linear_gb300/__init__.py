@@ -28,6 +28,7 @@ INF32 = 1 << 30
 LIB_PATH = _build.LIB_PATH
 CLI_PATH = _build.CLI_PATH
 
+BATCH_CLASSES = 12
 TREE = 0x1
 TABLE = 0x2
 NOCHECK = 0x4
@@ -117,6 +118,8 @@ SIGNATURES = {
     "emv_solve_dev": (ctypes.c_int, [_P, ctypes.POINTER(_Graph), _P, _I32, _I32, ctypes.POINTER(_Result), _P]),
     "emv_sssp": (ctypes.c_int, [_P, ctypes.POINTER(_Graph), _I32, _P, ctypes.POINTER(ctypes.c_float), _P]),
     "emv_batch_solve": (ctypes.c_int, [_P, ctypes.POINTER(_Instance), _I32, _P, ctypes.POINTER(_BatchStats), _P]),
+    "emv_batch_autotune": (ctypes.c_int, [_P, ctypes.POINTER(_Instance), _I32, _P, _P]),
+    "emv_batch_set_tuning": (ctypes.c_int, [_P, _P, _I32]),
     "emv_server_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.POINTER(_ServerOpts)]),
     "emv_server_submit": (ctypes.c_int, [_P, ctypes.POINTER(_Graph), _P, _I32, ctypes.POINTER(_I64)]),
     "emv_server_poll": (ctypes.c_int, [_P, _I64, ctypes.POINTER(_I64), ctypes.POINTER(ctypes.c_double)]),
@@ -355,14 +358,30 @@ class Solver:
         _check(self._lib.emv_sssp(self._ctx, ctypes.byref(cg), source, dist.ctypes.data, ctypes.byref(ms), stream))
         return dist, float(ms.value)
 
-    def batch_solve(self, graphs: Sequence[Csr], stream: Optional[int] = None) -> tuple[np.ndarray, dict]:
-        """Many independent instances in one persistent launch per level (emv_batch_solve)."""
-        count = len(graphs)
-        insts = (_Instance * count)()
+    @staticmethod
+    def _instances(graphs: Sequence[Csr]):
+        insts = (_Instance * len(graphs))()
         for i, g in enumerate(graphs):
             insts[i].g = g.c_graph()
             insts[i].terminals = g.terminals.ctypes.data
             insts[i].k = g.k
+        return insts
+
+    def batch_autotune(self, graphs: Sequence[Csr], stream: Optional[int] = None) -> np.ndarray:
+        """Tunes the batched launch per instance class (emv_batch_autotune); returns the rcap table."""
+        insts = self._instances(graphs)
+        out = np.zeros(BATCH_CLASSES, np.int32)
+        _check(self._lib.emv_batch_autotune(self._ctx, insts, len(graphs), out.ctypes.data, stream))
+        return out
+
+    def batch_set_tuning(self, rcap) -> None:
+        r = np.ascontiguousarray(rcap, dtype=np.int32)
+        _check(self._lib.emv_batch_set_tuning(self._ctx, r.ctypes.data, int(r.shape[0])))
+
+    def batch_solve(self, graphs: Sequence[Csr], stream: Optional[int] = None) -> tuple[np.ndarray, dict]:
+        """Many independent instances in one persistent launch (emv_batch_solve)."""
+        count = len(graphs)
+        insts = self._instances(graphs)
         costs = np.zeros(count, np.int64)
         st = _BatchStats()
         _check(self._lib.emv_batch_solve(self._ctx, insts, count, costs.ctypes.data, ctypes.byref(st), stream))

@@ -1,0 +1,200 @@
+"""Batched and serving workloads of bench.py.
+
+batched: 4096 independent instances of the mixed distribution (n log-uniform
+  in [64, 4096], degree {3,4,6,8}, k uniform in [4, 10], weights [1, 1000],
+  about 10% group instances; instance i is generated from seed base + i),
+  solved by one persistent, graph-captured launch; compared with the plain
+  one-instance-at-a-time GPU solve and with the reference on the host cores
+  (one single-threaded process per core).
+serve: Poisson arrivals of instances from the same distribution plus 2%
+  large ones (n = 2^17, degree 8, k = 12), admitted by table footprint
+  against a 150 GB budget; p50/p99 latency and solves/s per arrival rate,
+  and the plain sequential GPU solves/s of the same stream.
+"""
+from __future__ import annotations
+
+import os
+import random
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+
+from . import Csr, Server, Solver, StpInstance
+
+MIXED_BASE = 20250301
+LARGE = dict(n=1 << 17, degree=8, wmin=1, wmax=1000, k=12)
+
+
+def shard(count: int, rank: int, world: int) -> range:
+    """Contiguous share of `count` instances for `rank` of `world` replicas."""
+    per, rem = divmod(count, world)
+    start = rank * per + min(rank, rem)
+    return range(start, start + per + (1 if rank < rem else 0))
+
+
+def mixed_instances(indices) -> list[Csr]:
+    return [Csr.from_stp(StpInstance.mixed(MIXED_BASE, i)) for i in indices]
+
+
+def percentile(xs, q):
+    xs = sorted(xs)
+    if not xs:
+        return None
+    i = min(len(xs) - 1, max(0, int(round(q / 100.0 * (len(xs) - 1)))))
+    return xs[i]
+
+
+def _reference_throughput(graphs_idx, seconds_budget: float = 20.0) -> dict:
+    """The reference's emv_kernel (oracle/_ref) in throughput mode: one
+    single-threaded process per host core over a sample of the instances."""
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import oracle
+
+    oracle.build(reference=True)
+    cores = os.cpu_count() or 1
+    with tempfile.TemporaryDirectory() as tmp:
+        paths = []
+        for i in graphs_idx:
+            p = os.path.join(tmp, f"i{i}.stp")
+            StpInstance.mixed(MIXED_BASE, i).write(p)
+            paths.append(p)
+        kind = "reference" if oracle.reference_available() else "port"
+
+        def one(p):
+            t0 = time.perf_counter()
+            if kind == "reference":
+                oracle.ref_emv(p, threads=1)
+            else:
+                g = Csr.from_stp(StpInstance.from_file(p))
+                oracle.emv_table(g.n, g.row_ptr, g.col, g.w, g.terminals, threads=1)
+            return time.perf_counter() - t0
+
+        t0 = time.perf_counter()
+        done = 0
+        with ThreadPoolExecutor(max_workers=cores) as ex:
+            for _ in ex.map(one, paths):
+                done += 1
+        wall = time.perf_counter() - t0
+    return {"value": done / wall, "unit": "solves/s", "cores": cores, "kind": kind,
+            "sample": f"{done} instances of the same distribution, one single-threaded process per core"}
+
+
+def run_batched(args, dist) -> dict:
+    import torch
+
+    dev = torch.device("cuda", dist.local)
+    torch.cuda.set_device(dev)
+    idx = shard(args.batch_count * dist.world, dist.rank, dist.world)  # weak scaling: count per GPU
+    graphs = mixed_instances(idx)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    solver = Solver(dist.local)
+    tuning = solver.batch_autotune(graphs, stream=stream)
+    for _ in range(max(3, args.warmup)):
+        costs, st = solver.batch_solve(graphs, stream=stream)
+    dist.barrier()
+    dev_ms, wall = [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        c2, st = solver.batch_solve(graphs, stream=stream)
+        wall.append(time.perf_counter() - t0)
+        dev_ms.append(st["total_ms"])
+        assert np.array_equal(c2, costs)
+    dist.barrier()
+    ms = dist.max(statistics.median(dev_ms))
+    e2e_s = dist.max(statistics.median(wall))
+    # plain one-at-a-time GPU solves on a sample, same instances
+    sample = graphs[:256]
+    for g in sample[:8]:
+        solver.solve(g, check=False, stream=stream)
+    t0 = time.perf_counter()
+    plain_costs = [solver.solve(g, check=False, stream=stream).cost for g in sample]
+    plain_rate = len(sample) / (time.perf_counter() - t0)
+    assert plain_costs == [int(x) for x in costs[:len(sample)]]
+    solver.close()
+    count = len(graphs) * dist.world
+    out = {"metric": "solves/s", "value": round(count / (ms / 1000.0), 1), "unit": "solves/s",
+           "n_gpus": dist.world, "steps": args.steps, "warmup": max(3, args.warmup),
+           "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "int32", "data": "synthetic (seeded mixed distribution)",
+           "config": {"workload": f"batched: {len(graphs)} mixed instances per GPU in one persistent launch",
+                      "table_bytes": st["table_bytes"], "relax_rows": st["relax_rows"],
+                      "autotuned_rcap_by_class": [int(x) for x in tuning]},
+           "e2e": {"value": round(count / e2e_s, 1), "unit": "solves/s",
+                   "h2d_bytes_per_step": int(sum(4 * (g.n + 1) + 8 * g.arcs + 4 * g.k for g in graphs)),
+                   "d2h_bytes_per_step": 8 * len(graphs) + 4},
+           "plain_gpu_one_at_a_time": {"value": round(plain_rate, 1), "unit": "solves/s",
+                                       "sample": f"first {len(sample)} instances, emv_solve each"},
+           "batched_vs_plain": round(count / (ms / 1000.0) / plain_rate, 1)}
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = _reference_throughput(range(0, 256))
+    return out
+
+
+def run_serve(args, dist) -> dict | None:
+    """Poisson request stream against the continuous-batching server."""
+    import torch
+
+    if dist.rank != 0:
+        return None
+    torch.cuda.set_device(dist.local)
+    rng = random.Random(12345)
+    nreq = args.serve_requests
+    kinds = ["large" if rng.random() < 0.02 else "mixed" for _ in range(nreq)]
+    large_cache = {}
+    stream = []
+    for i, kd in enumerate(kinds):
+        if kd == "large":
+            key = len(large_cache) % 4  # four distinct large instances, reused
+            if key not in large_cache:
+                large_cache[key] = Csr.from_stp(StpInstance.regular(seed=1000 + key, **LARGE))
+            stream.append(large_cache[key])
+        else:
+            stream.append(Csr.from_stp(StpInstance.mixed(MIXED_BASE, i)))
+    with Solver(dist.local) as s:
+        want = [s.solve(g, check=False).cost for g in stream[:64]]
+        t0 = time.perf_counter()
+        n_plain = min(len(stream), 400)
+        for g in stream[:n_plain]:
+            s.solve(g, check=False)
+        plain_rate = n_plain / (time.perf_counter() - t0)
+    results = []
+    for rate in [float(x) for x in args.serve_rates.split(",")]:
+        with Server(dist.local, hbm_budget_bytes=150 * 10**9, max_slots=4096, large_n=65536) as srv:
+            ids = []
+            t_start = time.perf_counter()
+            next_t = t_start
+            for g in stream:
+                next_t += rng.expovariate(rate)
+                delay = next_t - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                ids.append(srv.submit(g))
+            lat = []
+            costs = []
+            for r in ids:
+                c, l_ms = srv.wait(r, 3600)
+                costs.append(c)
+                lat.append(l_ms)
+            wall = time.perf_counter() - t_start
+            st = srv.stats()
+        assert costs[:64] == want, "served costs differ from single solves"
+        small = [l for l, kd in zip(lat, kinds) if kd == "mixed"]
+        results.append({"arrival_rate": rate, "solves_per_s": round(len(ids) / wall, 1),
+                        "p50_ms": round(percentile(lat, 50), 3), "p99_ms": round(percentile(lat, 99), 3),
+                        "p99_small_ms": round(percentile(small, 99), 3), "waves": st["waves"],
+                        "peak_resident": st["peak_resident"], "peak_bytes": st["peak_bytes"]})
+    best = max(r["solves_per_s"] for r in results)
+    return {"metric": "solves/s", "value": best, "unit": "solves/s", "n_gpus": 1, "steps": len(results),
+            "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic (mixed distribution + 2% n=2^17 k=12)",
+            "config": {"workload": f"serving: {nreq} Poisson arrivals per rate, budget 150 GB"},
+            "rates": results,
+            "plain_gpu_sequential": {"value": round(plain_rate, 1), "unit": "solves/s",
+                                     "sample": f"first {n_plain} requests of the stream, emv_solve each"},
+            "served_vs_plain": round(best / plain_rate, 1)}

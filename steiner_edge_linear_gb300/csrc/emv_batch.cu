@@ -173,21 +173,25 @@ int batch_pack(emv_ctx *c, const emv_instance *inst, const std::vector<int32_t> 
 {
     const int32_t count = (int32_t)order.size();
     pk.desc.resize((size_t)count);
+    pk.row_off.resize((size_t)count);
+    pk.arc_off.resize((size_t)count);
+    pk.term_off.resize((size_t)count);
+    pk.table_off.resize((size_t)count);
     int64_t rows = 0, arcs = 0, terms = 0, words = 0;
     for (int32_t j = 0; j < count; j++) {
         const emv_instance &I = inst[order[(size_t)j]];
         BatchInst &d = pk.desc[(size_t)j];
+        std::memset(&d, 0, sizeof(d));
         d.n = I.g.n;
         d.k = I.k;
         d.rcap = batch_rcap_for(c, I.g.n, I.k);
         d.orig = order[(size_t)j];
-        d.row_off = rows;
-        d.arc_off = arcs;
-        d.table_off = words;
-        d.term_off = (int32_t)terms;
         d.lo = lo;
         d.hi = hi < 0 ? I.k : hi;
-        d.pad = 0;
+        pk.row_off[(size_t)j] = rows;
+        pk.arc_off[(size_t)j] = arcs;
+        pk.term_off[(size_t)j] = terms;
+        pk.table_off[(size_t)j] = words;
         rows += I.g.n + 1;
         arcs += I.g.arcs;
         terms += I.k;
@@ -219,10 +223,10 @@ int batch_pack(emv_ctx *c, const emv_instance *inst, const std::vector<int32_t> 
     BatchInst *hdesc = (BatchInst *)(((uintptr_t)(hterm + terms) + 15) & ~(uintptr_t)15);
     for (int32_t j = 0; j < count; j++) {
         const emv_instance &I = inst[order[(size_t)j]];
-        const BatchInst &d = pk.desc[(size_t)j];
-        std::memcpy(hrow + d.row_off, I.g.row_ptr, sizeof(int32_t) * ((size_t)I.g.n + 1));
-        for (int64_t e = 0; e < I.g.arcs; e++) hadj[d.arc_off + e] = make_int2(I.g.col[e], I.g.w[e]);
-        std::memcpy(hterm + d.term_off, I.terminals, sizeof(int32_t) * (size_t)I.k);
+        std::memcpy(hrow + pk.row_off[(size_t)j], I.g.row_ptr, sizeof(int32_t) * ((size_t)I.g.n + 1));
+        int2 *ha = hadj + pk.arc_off[(size_t)j];
+        for (int64_t e = 0; e < I.g.arcs; e++) ha[e] = make_int2(I.g.col[e], I.g.w[e]);
+        std::memcpy(hterm + pk.term_off[(size_t)j], I.terminals, sizeof(int32_t) * (size_t)I.k);
     }
     std::memcpy(hdesc, pk.desc.data(), sizeof(BatchInst) * (size_t)count);
     pk.h_row = hrow;
@@ -243,6 +247,14 @@ int batch_upload(emv_ctx *c, BatchPack &pk, cudaStream_t st)
     if (!r) r = dev_reserve(c->b_ctrl, 64);
     if (!r) r = prepare_batch_subsets(c, st);
     if (r) return r;
+    for (int32_t j = 0; j < pk.count; j++) {
+        BatchInst &d = pk.h_desc[j];
+        d.row_ptr = (const int32_t *)c->b_row.ptr + pk.row_off[(size_t)j];
+        d.adj = (const int2 *)c->b_adj.ptr + pk.arc_off[(size_t)j];
+        d.terms = (const int32_t *)c->b_term.ptr + pk.term_off[(size_t)j];
+        d.table = (int32_t *)c->b_table.ptr + pk.table_off[(size_t)j];
+        pk.desc[(size_t)j] = d;
+    }
     CUDA_TRY(cudaMemcpyAsync(c->b_row.ptr, pk.h_row, sizeof(int32_t) * (size_t)pk.rows, cudaMemcpyHostToDevice, st));
     if (pk.arcs > 0)
         CUDA_TRY(cudaMemcpyAsync(c->b_adj.ptr, pk.h_adj, sizeof(int2) * (size_t)pk.arcs, cudaMemcpyHostToDevice, st));
@@ -260,10 +272,6 @@ BatchArgs batch_args(emv_ctx *c, const BatchPack &pk)
     std::memset(&a, 0, sizeof(a));  // padding included: the graph cache compares bytes
     a.inst = (const BatchInst *)c->b_desc.ptr;
     a.count = pk.count;
-    a.row_ptr = (const int32_t *)c->b_row.ptr;
-    a.adj = (const int2 *)c->b_adj.ptr;
-    a.terms = (const int32_t *)c->b_term.ptr;
-    a.tables = (int32_t *)c->b_table.ptr;
     a.xs = (const uint32_t *)c->bxs.ptr;
     a.xs_off = (const int32_t *)c->bxs_off.ptr;
     a.costs = (int64_t *)c->b_costs.ptr;

@@ -14,41 +14,10 @@
 // The table of an instance is int32 row-major with ld = n.
 #pragma once
 
+#include "emv_batch_types.h"
 #include "emv_common.cuh"
 
 namespace emv {
-
-constexpr int BATCH_THREADS = 1024;
-constexpr int BATCH_KMAX = 12;
-constexpr int32_t BATCH_SMEM_BYTES = 200 * 1024;
-
-struct BatchInst {
-    int32_t n;
-    int32_t k;
-    int32_t rcap;       // relaxation rows per chunk (autotuned, power of two <= 32)
-    int32_t orig;       // position in the caller's order
-    int64_t row_off;    // into BatchArgs::row_ptr (n + 1 entries, 0-based arcs)
-    int64_t arc_off;    // into BatchArgs::adj
-    int64_t table_off;  // into BatchArgs::tables (int32 units)
-    int32_t term_off;   // into BatchArgs::terms
-    int32_t lo;         // first level to run (1..k)
-    int32_t hi;         // last level to run (lo..k)
-    int32_t pad;
-};
-
-struct BatchArgs {
-    const BatchInst *inst;
-    int32_t count;
-    const int32_t *row_ptr;
-    const int2 *adj;
-    const int32_t *terms;
-    int32_t *tables;
-    const uint32_t *xs;      // subsets by level for k = 1..BATCH_KMAX, concatenated
-    const int32_t *xs_off;   // xs_off[k * (BATCH_KMAX + 2) + m]: start of level m of k
-    int64_t *costs;          // by orig; written when hi == k
-    uint32_t *queue;         // [0] next work item
-    uint32_t *err;
-};
 
 __device__ __forceinline__ int32_t xs_start(const BatchArgs &a, int32_t k, int32_t m)
 {
@@ -154,10 +123,10 @@ __device__ bool batch_relax(const BatchArgs &a, int32_t *table, int32_t n, const
 __device__ void batch_solve_one(const BatchArgs &a, const BatchInst &I, int32_t *S)
 {
     const int32_t n = I.n, k = I.k;
-    int32_t *table = a.tables + I.table_off;
-    const int32_t *row_ptr = a.row_ptr + I.row_off;
-    const int2 *adj = a.adj + I.arc_off;
-    const int32_t *terms = a.terms + I.term_off;
+    int32_t *table = I.table;
+    const int32_t *row_ptr = I.row_ptr;
+    const int2 *adj = I.adj;
+    const int32_t *terms = I.terms;
     bool ok = true;
     for (int32_t m = I.lo; m <= I.hi && ok; m++) {
         if (m == 1) {

@@ -4,11 +4,12 @@
 #include <chrono>
 #include <vector>
 
-#include "emv_batch.cuh"
+#include "emv_batch_types.h"
 #include "emv_solver.h"
 
 struct BatchPack {
     std::vector<emv::BatchInst> desc;  // in launch order
+    std::vector<int64_t> row_off, arc_off, term_off, table_off;  // into the packed device buffers
     int64_t rows = 0, arcs = 0, terms = 0, table_words = 0;
     int32_t count = 0;
     int32_t rcap_used = 0;

@@ -84,9 +84,12 @@ extern "C" int emv_create(emv_ctx **out, int32_t device)
     if (!c) return emv_fail(EMV_ERR_OOM, "ctx");
     c->device = device;
     c->sms = prop.multiProcessorCount;
-    int per_sm = 0;
-    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_relax_chunk, RELAX_THREADS, 0));
-    c->relax_blocks_max = std::max(1, per_sm) * c->sms;
+    const void *relax_fns[3] = {(const void *)k_relax<1>, (const void *)k_relax<2>, (const void *)k_relax<4>};
+    for (int i = 0; i < 3; i++) {
+        int per_sm = 0;
+        CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, relax_fns[i], RELAX_THREADS, 0));
+        c->relax_blocks_max[i] = std::max(1, per_sm) * c->sms;
+    }
     int st = dev_reserve(c->ctrl, sizeof(uint32_t) * C_WORDS);
     if (!st) st = dev_reserve(c->stat, sizeof(DevStat));
     if (!st) {
@@ -107,7 +110,7 @@ extern "C" int emv_destroy(emv_ctx *c)
     if (!c) return EMV_OK;
     cudaSetDevice(c->device);
     cudaDeviceSynchronize();
-    for (DevBuf *b : {&c->ctrl, &c->stat, &c->scratch, &c->act, &c->adj, &c->xs, &c->terms, &c->g_row,
+    for (DevBuf *b : {&c->ctrl, &c->stat, &c->scratch, &c->act, &c->adj, &c->xs, &c->mpairs, &c->movr, &c->terms, &c->g_row,
                       &c->g_col, &c->g_w, &c->table, &c->tb_edges, &c->tb_out, &c->tb_work})
         dev_release(*b);
     for (int i = 0; i < MAX_EVENTS; i++)
@@ -125,7 +128,8 @@ static int grid_for(int64_t work, int threads, int cap)
     return (int)std::max<int64_t>(1, std::min<int64_t>(g, cap));
 }
 
-// Launches the relaxation of one chunk of rows (cooperative, persistent).
+// Launches the relaxation of one chunk of at most CHUNK_ROWS rows
+// (cooperative, persistent); the record width follows the row count.
 int launch_relax(emv_ctx *c, const int32_t *row_ptr, const int2 *adj, int32_t n, int64_t ld, int32_t *table,
                  const uint32_t *rows, int32_t nrows, const int32_t *terms, int32_t level1, cudaStream_t st)
 {
@@ -145,13 +149,15 @@ int launch_relax(emv_ctx *c, const int32_t *row_ptr, const int2 *adj, int32_t n,
     a.ctrl = (uint32_t *)c->ctrl.ptr;
     a.stat = (DevStat *)c->stat.ptr;
     a.max_sweeps = n + 1;
-    // One warp per vertex is enough; small graphs use fewer blocks (cheaper barriers).
-    const int blocks = std::min(c->relax_blocks_max, std::max(1, (n + 7) / 8));
+    const int vi = nrows <= 32 ? 0 : nrows <= 64 ? 1 : 2;
+    const void *fn = vi == 0 ? (const void *)k_relax<1> : vi == 1 ? (const void *)k_relax<2> : (const void *)k_relax<4>;
+    // A warp per 32 vertices is enough; small graphs use fewer blocks (cheaper barriers).
+    const int vpb = 32 * (RELAX_THREADS / 32);
+    const int blocks = std::min(c->relax_blocks_max[vi], std::max(1, (n + vpb - 1) / vpb));
     CUDA_TRY(cudaMemsetAsync(a.ctrl, 0, sizeof(uint32_t) * C_WORDS, st));
     void *args[] = {&a};
-    CUDA_TRY(cudaLaunchCooperativeKernel((const void *)k_relax_chunk, dim3(blocks), dim3(RELAX_THREADS), args, 0, st));
-    k_collect_err<<<1, 32, 0, st>>>(a.ctrl, a.stat);
-    c->launches += 3;
+    CUDA_TRY(cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(RELAX_THREADS), args, 0, st));
+    c->launches += 2;
     return EMV_OK;
 }
 
@@ -163,6 +169,9 @@ int reserve_relax(emv_ctx *c, int32_t n)
     return st;
 }
 
+constexpr int32_t MERGE_SMEM_BYTES = 220 * 1024;
+constexpr int32_t MERGE_SMEM_KMAX = 15;  // staged slots must fit 16 bits
+
 int prepare_subsets(emv_ctx *c, int32_t k, cudaStream_t st)
 {
     if (c->xs_k == k) return EMV_OK;
@@ -171,8 +180,91 @@ int prepare_subsets(emv_ctx *c, int32_t k, cudaStream_t st)
     if (r) return r;
     CUDA_TRY(cudaMemcpyAsync(c->xs.ptr, c->xs_host.data(), sizeof(uint32_t) * c->xs_host.size(),
                              cudaMemcpyHostToDevice, st));
+    // Pair and override slot lists of the shared-memory merge (level order).
+    c->mpair_base.assign((size_t)k + 2, 0);
+    c->movr_base.assign((size_t)k + 2, 0);
+    std::vector<uint32_t> pairs, ovr;
+    if (k <= MERGE_SMEM_KMAX) {
+        std::vector<uint32_t> lidx((size_t)1 << k, 0);
+        for (size_t i = 0; i < c->xs_host.size(); i++) lidx[c->xs_host[i]] = (uint32_t)i;
+        for (int32_t m = 2; m <= k; m++) {
+            c->mpair_base[(size_t)m] = (int64_t)pairs.size();
+            c->movr_base[(size_t)m] = (int64_t)ovr.size();
+            for (int64_t i = c->xs_off[(size_t)m]; i < c->xs_off[(size_t)m + 1]; i++) {
+                const uint32_t X = c->xs_host[(size_t)i];
+                const uint32_t low = X & (0u - X), rest = X ^ low;
+                uint32_t sm = 0;
+                do {
+                    const uint32_t Y = low | sm;
+                    pairs.push_back(lidx[Y] | (lidx[X ^ Y] << 16));
+                    sm = (sm - rest) & rest;
+                } while (sm != rest);
+                for (int32_t t = 0; t < k; t++)
+                    if (X >> t & 1u) ovr.push_back(((uint32_t)t << 16) | lidx[X ^ (1u << t)]);
+            }
+        }
+    }
+    if (!pairs.empty()) {
+        r = dev_reserve(c->mpairs, sizeof(uint32_t) * pairs.size());
+        if (!r) r = dev_reserve(c->movr, sizeof(uint32_t) * ovr.size());
+        if (r) return r;
+        CUDA_TRY(cudaMemcpyAsync(c->mpairs.ptr, pairs.data(), sizeof(uint32_t) * pairs.size(), cudaMemcpyHostToDevice,
+                                 st));
+        CUDA_TRY(cudaMemcpyAsync(c->movr.ptr, ovr.data(), sizeof(uint32_t) * ovr.size(), cudaMemcpyHostToDevice, st));
+    }
     CUDA_TRY(cudaStreamSynchronize(st));
     c->xs_k = k;
+    return EMV_OK;
+}
+
+template <int VB>
+static cudaError_t merge_smem_launch(emv_ctx *c, int32_t *table, int64_t ld, int32_t n, int32_t k, int32_t m,
+                                     const int32_t *d_terms, cudaStream_t st)
+{
+    const int64_t b = c->xs_off[(size_t)m], cnt = c->xs_off[(size_t)m + 1] - b;
+    const int32_t nstage = (int32_t)c->xs_off[(size_t)m];
+    const uint32_t *xs = (const uint32_t *)c->xs.ptr;
+    const size_t smem = sizeof(int32_t) * (size_t)nstage * VB;
+    const int32_t npairs = (1 << (m - 1)) - 1;
+    k_merge_smem<VB><<<(unsigned)((n + VB - 1) / VB), 1024, smem, st>>>(
+        table, ld, n, xs + b, (int32_t)cnt, xs, nstage, (const uint32_t *)c->mpairs.ptr + c->mpair_base[(size_t)m],
+        npairs, (const uint32_t *)c->movr.ptr + c->movr_base[(size_t)m], m, d_terms);
+    (void)k;
+    return cudaGetLastError();
+}
+
+// Merge of level m: the shared-memory kernel with the widest vertex block
+// whose staging fits, else the direct kernel (k above MERGE_SMEM_KMAX).
+int launch_merge(emv_ctx *c, int32_t *table, int64_t ld, int32_t n, int32_t k, int32_t m, const int32_t *d_terms,
+                 cudaStream_t st)
+{
+    if (!c->merge_attr) {
+        const void *fns[6] = {(const void *)k_merge_smem<32>, (const void *)k_merge_smem<16>,
+                              (const void *)k_merge_smem<8>, (const void *)k_merge_smem<4>,
+                              (const void *)k_merge_smem<2>, (const void *)k_merge_smem<1>};
+        for (const void *f : fns)
+            CUDA_TRY(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, MERGE_SMEM_BYTES));
+        c->merge_attr = true;
+    }
+    const int64_t nstage = c->xs_off[(size_t)m];
+    cudaError_t e = cudaSuccess;
+    c->launches++;
+    if (k <= MERGE_SMEM_KMAX) {
+        const int64_t row_bytes = nstage * 4;
+        if (row_bytes * 32 <= MERGE_SMEM_BYTES) e = merge_smem_launch<32>(c, table, ld, n, k, m, d_terms, st);
+        else if (row_bytes * 16 <= MERGE_SMEM_BYTES) e = merge_smem_launch<16>(c, table, ld, n, k, m, d_terms, st);
+        else if (row_bytes * 8 <= MERGE_SMEM_BYTES) e = merge_smem_launch<8>(c, table, ld, n, k, m, d_terms, st);
+        else if (row_bytes * 4 <= MERGE_SMEM_BYTES) e = merge_smem_launch<4>(c, table, ld, n, k, m, d_terms, st);
+        else if (row_bytes * 2 <= MERGE_SMEM_BYTES) e = merge_smem_launch<2>(c, table, ld, n, k, m, d_terms, st);
+        else e = merge_smem_launch<1>(c, table, ld, n, k, m, d_terms, st);
+    } else {
+        const int64_t b = c->xs_off[(size_t)m], cnt = c->xs_off[(size_t)m + 1] - b;
+        const int32_t xper = (int32_t)std::min<int64_t>(cnt, 64);
+        dim3 grid((unsigned)((n + 31) / 32), (unsigned)((cnt + xper - 1) / xper));
+        k_merge<<<grid, 256, 0, st>>>(table, ld, n, (const uint32_t *)c->xs.ptr + b, (int32_t)cnt, xper, d_terms, k);
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess) return emv_fail(EMV_ERR_CUDA, "merge launch: %s", cudaGetErrorString(e));
     return EMV_OK;
 }
 
@@ -204,11 +296,8 @@ int run_dp(emv_ctx *c, int32_t n, const int32_t *row_ptr, const int2 *adj, int32
 
     for (int32_t m = 2; m <= k; m++) {
         const int64_t b = c->xs_off[(size_t)m], cnt = c->xs_off[(size_t)m + 1] - b;
-        const int32_t xper = (int32_t)std::min<int64_t>(cnt, 64);
-        dim3 grid((unsigned)((n + 31) / 32), (unsigned)((cnt + xper - 1) / xper));
-        k_merge<<<grid, 256, 0, st>>>(table, ld, n, xs + b, (int32_t)cnt, xper, d_terms, k);
-        c->launches++;
-        CUDA_TRY(cudaGetLastError());
+        r = launch_merge(c, table, ld, n, k, m, d_terms, st);
+        if (r) return r;
         CUDA_TRY(cudaEventRecord(E[ev++], st));  // merge end of level m
         for (int64_t off = 0; off < cnt; off += CHUNK_ROWS) {
             const int32_t rows = (int32_t)std::min<int64_t>(CHUNK_ROWS, cnt - off);

@@ -9,7 +9,7 @@
 //   k_fill        f_v = INF                          R:2243-2259
 //   k_pack_adj    (col, w) arcs packed as int2        R:794-826 (adjacency fill)
 //   k_merge       subset merge of one level           R:2068-2107
-//   k_relax_chunk multi-source closure of <= 32 rows  R:2109-2130, R:1762-1880
+//   k_relax<VEC>  multi-source closure of <= 32*VEC rows  R:2109-2130, R:1762-1880
 //                 (also the k level-1 SSSPs,          R:1988-2031)
 //   k_traceback   tree recovery by recomputation      R:1907-1944
 #pragma once
@@ -28,10 +28,10 @@ struct RelaxArgs {
     int64_t ld;
     int32_t *table;
     const uint32_t *rows;   // subsets of this chunk
-    int32_t nrows;          // <= CHUNK_ROWS
+    int32_t nrows;          // <= 32 * VEC of the launch
     const int32_t *terms;   // level-1 mode: row r is {r}, source terms[r]
     int32_t level1;
-    int32_t *scratch;       // vertex-major chunk buffer, n * CHUNK_ROWS int32
+    int32_t *scratch;       // vertex-major records, n * 32 * VEC int32
     uint8_t *act0;          // active flags, n bytes each
     uint8_t *act1;
     uint32_t *ctrl;         // C_WORDS words
@@ -121,56 +121,159 @@ __global__ void __launch_bounds__(256) k_merge(int32_t *__restrict__ table, int6
     }
 }
 
-// Multi-source shortest-path closure of up to 32 rows (R:2109-2130): for
+// Shared-memory subset merge of one level m (R:2068-2107).  Block = VB
+// consecutive vertices; it stages every row of size 1..m-1 for them once
+// (S[slot][VB], slot = position in level order), then computes all C(k,m)
+// rows of the level: a warp takes one subset X at a time, lane = (slice,
+// vertex) with 32/VB slices splitting X's pair list, combined by shuffles.
+// pairs[x * npairs + p] packs the staged slots of Y and X\Y of the p-th
+// unordered pair {Y, X\Y} of the x-th subset (Y holds the lowest terminal of
+// X); ovr[x * m + i] packs (terminal index << 16 | slot of X\{t}) for the
+// override of the virtual-source arcs (R:2099-2107).
+template <int VB>
+__global__ void __launch_bounds__(1024) k_merge_smem(int32_t *__restrict__ table, int64_t ld, int32_t n,
+                                                     const uint32_t *__restrict__ xs_level, int32_t cnt,
+                                                     const uint32_t *__restrict__ stage_rows, int32_t nstage,
+                                                     const uint32_t *__restrict__ pairs, int32_t npairs,
+                                                     const uint32_t *__restrict__ ovr, int32_t m,
+                                                     const int32_t *__restrict__ terms)
+{
+    extern __shared__ int32_t S[];
+    constexpr int G = 32 / VB;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int32_t v0 = blockIdx.x * VB;
+    for (int32_t idx = threadIdx.x; idx < nstage * VB; idx += blockDim.x) {
+        const int32_t i = idx / VB, j = idx - i * VB;
+        const int32_t v = v0 + j;
+        S[idx] = (v < n) ? __ldg(table + (int64_t)__ldg(stage_rows + i) * ld + v) : INF;
+    }
+    __syncthreads();
+    const int slice = lane / VB, j = lane % VB;
+    const int32_t v = v0 + j;
+    for (int32_t xi = warp; xi < cnt; xi += nw) {
+        const uint32_t *P = pairs + (int64_t)xi * npairs;
+        uint32_t acc = (uint32_t)INF, acc2 = (uint32_t)INF;
+        int32_t p = slice;
+        for (; p + G < npairs; p += 2 * G) {
+            const uint32_t q0 = __ldg(P + p), q1 = __ldg(P + p + G);
+            acc = min(acc, (uint32_t)S[(q0 & 0xffffu) * VB + j] + (uint32_t)S[(q0 >> 16) * VB + j]);
+            acc2 = min(acc2, (uint32_t)S[(q1 & 0xffffu) * VB + j] + (uint32_t)S[(q1 >> 16) * VB + j]);
+        }
+        if (p < npairs) {
+            const uint32_t q0 = __ldg(P + p);
+            acc = min(acc, (uint32_t)S[(q0 & 0xffffu) * VB + j] + (uint32_t)S[(q0 >> 16) * VB + j]);
+        }
+        acc = min(acc, acc2);
+#pragma unroll
+        for (int off = 16; off >= VB; off >>= 1) acc = min(acc, __shfl_xor_sync(FULL, acc, off));
+        if (slice == 0 && v < n) {
+            const uint32_t *O = ovr + (int64_t)xi * m;
+            for (int i = 0; i < m; i++) {
+                const uint32_t o = __ldg(O + i);
+                if (__ldg(terms + (o >> 16)) == v) acc = (uint32_t)S[(o & 0xffffu) * VB + j];
+            }
+            table[(int64_t)__ldg(xs_level + xi) * ld + v] = (int32_t)acc;
+        }
+    }
+}
+
+// Vector of VEC int32 (one lane's share of a vertex record).
+template <int VEC> struct IVec;
+template <> struct IVec<1> {
+    using T = int32_t;
+};
+template <> struct IVec<2> {
+    using T = int2;
+};
+template <> struct IVec<4> {
+    using T = int4;
+};
+
+__device__ __forceinline__ int32_t vmin(int32_t a, int32_t b) { return min(a, b); }
+__device__ __forceinline__ int2 vmin(int2 a, int2 b) { return make_int2(min(a.x, b.x), min(a.y, b.y)); }
+__device__ __forceinline__ int4 vmin(int4 a, int4 b)
+{
+    return make_int4(min(a.x, b.x), min(a.y, b.y), min(a.z, b.z), min(a.w, b.w));
+}
+__device__ __forceinline__ int32_t vadd(int32_t a, int32_t w) { return a + w; }
+__device__ __forceinline__ int2 vadd(int2 a, int32_t w) { return make_int2(a.x + w, a.y + w); }
+__device__ __forceinline__ int4 vadd(int4 a, int32_t w) { return make_int4(a.x + w, a.y + w, a.z + w, a.w + w); }
+__device__ __forceinline__ bool vlt(int32_t a, int32_t b) { return a < b; }
+__device__ __forceinline__ bool vlt(int2 a, int2 b) { return a.x < b.x || a.y < b.y; }
+__device__ __forceinline__ bool vlt(int4 a, int4 b) { return a.x < b.x || a.y < b.y || a.z < b.z || a.w < b.w; }
+template <typename T> __device__ __forceinline__ T vinf();
+template <> __device__ __forceinline__ int32_t vinf<int32_t>() { return INF; }
+template <> __device__ __forceinline__ int2 vinf<int2>() { return make_int2(INF, INF); }
+template <> __device__ __forceinline__ int4 vinf<int4>() { return make_int4(INF, INF, INF, INF); }
+
+// Multi-source shortest-path closure of up to 32*VEC rows (R:2109-2130): for
 // every row X of the chunk, d[X][v] = min over u of init[u] + dist(u, v).
 // One cooperative persistent launch:
-//   A. transpose the rows into a vertex-major buffer (vertex v: 32 ints, one
-//      128-byte line) -- in level-1 mode the rows are k single-source inits;
-//   B. frontier sweeps: a warp owns a vertex, lane r its row r; it pulls
-//      min over arcs (u, w) of d[u] + w with coalesced 128-byte gathers and
-//      writes in place (only the owner writes, values only decrease, so no
-//      atomics are needed); a vertex that decreased marks its neighbours
-//      active for the next sweep; sweeps end when one changes nothing
-//      (bounded by n + 1 sweeps, the Bellman-Ford bound);
+//   A. transpose the rows into a vertex-major buffer: vertex v owns one
+//      record of R = 32*VEC int32 (lane l holds rows l*VEC .. l*VEC+VEC-1);
+//      in level-1 mode the rows are the k single-source initialisations;
+//   B. frontier sweeps: a warp takes 32 vertices at once, reads their active
+//      flags and CSR bounds with one coalesced load each, and for every
+//      active vertex pulls min over its arcs (u, w) of rec[u] + w -- one
+//      coalesced 128*VEC-byte gather per arc, 2 KB in flight per warp -- and writes
+//      the record in place.  Only the owner writes a record and values only
+//      decrease, so no atomics are needed; a vertex that decreased marks its
+//      neighbours active for the next sweep.  Sweeps end when one changes
+//      nothing (bounded by n + 1, the Bellman-Ford bound);
 //   C. transpose back into the table rows.
-// Scratch reads use ld.global.cg (L2, never a stale L1 line).
-__global__ void __launch_bounds__(RELAX_THREADS) k_relax_chunk(RelaxArgs a)
+// Buffer reads use ld.global.cg (L2), never a stale L1 line.
+template <int VEC>
+__global__ void __launch_bounds__(RELAX_THREADS, 2) k_relax(RelaxArgs a)
 {
+    using V = typename IVec<VEC>::T;
+    constexpr int R = 32 * VEC;
+    constexpr int GROUP = VEC == 4 ? 4 : 8;  // gathers in flight per warp: 2 KB for VEC >= 2
     __shared__ int32_t tile[32][33];
     __shared__ int s_ok;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwb = blockDim.x >> 5;
     const int32_t n = a.n;
     const int32_t ntiles = (n + 31) >> 5;
     const int32_t nrows = a.nrows;
+    int32_t *buf = a.scratch;
 
-    // ---- A: rows -> vertex-major buffer
+    // ---- A: rows -> vertex-major records
     for (int32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int32_t v = t * 32 + lane;
-        for (int r = warp; r < 32; r += nwb) {
-            int32_t x = INF;
-            if (r < nrows && v < n) {
-                if (a.level1) x = (v == __ldg(a.terms + r)) ? 0 : INF;
-                else x = __ldcg(a.table + (int64_t)__ldg(a.rows + r) * a.ld + v);
+        for (int g = 0; g < VEC; g++) {
+            for (int r = warp; r < 32; r += nwb) {
+                const int32_t row = g * 32 + r;
+                int32_t x = INF;
+                if (row < nrows && v < n) {
+                    if (a.level1) x = (v == __ldg(a.terms + row)) ? 0 : INF;
+                    else x = __ldcg(a.table + (int64_t)__ldg(a.rows + row) * a.ld + v);
+                }
+                tile[r][lane] = x;
             }
-            tile[r][lane] = x;
+            __syncthreads();
+            // record of vertex vv: element (l*VEC + j) holds row l*VEC + j
+            for (int vv = warp; vv < 32; vv += nwb) {
+                const int32_t v2 = t * 32 + vv;
+                if (v2 < n) {
+                    __stcg(buf + (int64_t)v2 * R + g * 32 + lane, tile[lane][vv]);  // element e holds row e
+                }
+            }
+            __syncthreads();
         }
-        __syncthreads();
-        for (int vv = warp; vv < 32; vv += nwb) {
-            const int32_t v2 = t * 32 + vv;
-            if (v2 < n) __stcg(a.scratch + (int64_t)v2 * 32 + lane, tile[lane][vv]);
-        }
-        __syncthreads();
     }
     for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
         a.act0[v] = 1;
         a.act1[v] = 0;
     }
-    if (!grid_barrier(a.ctrl, &s_ok)) return;
+    if (!grid_barrier(a.ctrl, &s_ok)) {
+        if (threadIdx.x == 0) atomicOr(&a.stat->err, a.ctrl[C_ERR]);
+        return;
+    }
 
     // ---- B: frontier sweeps
     const int32_t gw = (int32_t)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int32_t nwg = (int32_t)((gridDim.x * blockDim.x) >> 5);
     volatile uint32_t *vctrl = a.ctrl;
+    const V *recs = reinterpret_cast<const V *>(buf);
     int32_t s = 0;
     bool converged = false;
     for (; s < a.max_sweeps; s++) {
@@ -178,35 +281,53 @@ __global__ void __launch_bounds__(RELAX_THREADS) k_relax_chunk(RelaxArgs a)
         uint8_t *nxt = (s & 1) ? a.act0 : a.act1;
         if (blockIdx.x == 0 && threadIdx.x == 0) vctrl[C_SLOT0 + (s + 1) % 3] = 0;
         bool any = false;
-        for (int32_t v = gw; v < n; v += nwg) {
-            if (__ldcg(cur + v) == 0) continue;
-            if (lane == 0) cur[v] = 0;
-            const int32_t beg = __ldg(a.row_ptr + v), end = __ldg(a.row_ptr + v + 1);
-            int32_t *sv = a.scratch + (int64_t)v * 32 + lane;
-            const int32_t old = __ldcg(sv);
-            int32_t acc = old;
-            for (int32_t e0 = beg; e0 < end; e0 += 32) {
-                const int32_t e = e0 + lane;
-                int2 arc = make_int2(0, 0);
-                if (e < end) arc = __ldg(a.adj + e);
-                const int cntj = min(32, end - e0);
-#pragma unroll 4
-                for (int j = 0; j < cntj; j++) {
-                    const int32_t u = __shfl_sync(FULL, arc.x, j);
-                    const int32_t wt = __shfl_sync(FULL, arc.y, j);
-                    acc = min(acc, __ldcg(a.scratch + (int64_t)u * 32 + lane) + wt);
+        for (int32_t blk = gw; blk < ntiles; blk += nwg) {
+            const int32_t v = blk * 32 + lane;
+            const bool f = v < n && __ldcg(cur + v) != 0;
+            unsigned act = __ballot_sync(FULL, f);
+            if (!act) continue;
+            if (f) cur[v] = 0;
+            const int32_t rp0 = v < n ? __ldg(a.row_ptr + v) : 0;
+            const int32_t rp1 = v < n ? __ldg(a.row_ptr + v + 1) : 0;
+            while (act) {
+                const int j = __ffs(act) - 1;
+                act &= act - 1;
+                const int32_t vv = blk * 32 + j;
+                const int32_t beg = __shfl_sync(FULL, rp0, j), end = __shfl_sync(FULL, rp1, j);
+                V *mine = reinterpret_cast<V *>(buf + (int64_t)vv * R) + lane;
+                const V old = __ldcg(mine);
+                V acc = old;
+                for (int32_t e0 = beg; e0 < end; e0 += 32) {
+                    int2 arc = make_int2(0, 0);
+                    if (e0 + lane < end) arc = __ldg(a.adj + e0 + lane);
+                    const int cnt = min(32, end - e0);
+                    for (int g = 0; g < cnt; g += GROUP) {
+                        V val[GROUP];
+                        int32_t wt[GROUP];
+#pragma unroll
+                        for (int i = 0; i < GROUP; i++) {
+                            const int32_t u = __shfl_sync(FULL, arc.x, (g + i) & 31);
+                            wt[i] = __shfl_sync(FULL, arc.y, (g + i) & 31);
+                            val[i] = (g + i < cnt) ? __ldcg(recs + (int64_t)u * 32 + lane) : vinf<V>();
+                        }
+#pragma unroll
+                        for (int i = 0; i < GROUP; i++) acc = vmin(acc, vadd(val[i], wt[i]));
+                    }
                 }
-            }
-            const bool dec = acc < old;
-            if (dec) __stcg(sv, acc);
-            if (__ballot_sync(FULL, dec)) {
-                any = true;
-                for (int32_t e = beg + lane; e < end; e += 32) nxt[__ldg(&a.adj[e].x)] = 1;
+                const bool dec = vlt(acc, old);
+                if (dec) __stcg(mine, acc);
+                if (__ballot_sync(FULL, dec)) {
+                    any = true;
+                    for (int32_t e = beg + lane; e < end; e += 32) nxt[__ldg(&a.adj[e].x)] = 1;
+                }
             }
         }
         any = __syncthreads_or(any);
         if (any && threadIdx.x == 0) vctrl[C_SLOT0 + s % 3] = 1;
-        if (!grid_barrier(a.ctrl, &s_ok)) return;
+        if (!grid_barrier(a.ctrl, &s_ok)) {
+            if (threadIdx.x == 0) atomicOr(&a.stat->err, a.ctrl[C_ERR]);
+            return;
+        }
         if (vctrl[C_SLOT0 + s % 3] == 0) {
             converged = true;
             s++;
@@ -219,24 +340,23 @@ __global__ void __launch_bounds__(RELAX_THREADS) k_relax_chunk(RelaxArgs a)
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.stat->sweeps, (unsigned long long)s);
 
-    // ---- C: vertex-major buffer -> rows
+    // ---- C: vertex-major records -> rows
     for (int32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        for (int vv = warp; vv < 32; vv += nwb) {
-            const int32_t v2 = t * 32 + vv;
-            tile[vv][lane] = (v2 < n) ? __ldcg(a.scratch + (int64_t)v2 * 32 + lane) : INF;
+        for (int g = 0; g < VEC; g++) {
+            for (int vv = warp; vv < 32; vv += nwb) {
+                const int32_t v2 = t * 32 + vv;
+                tile[vv][lane] = (v2 < n) ? __ldcg(buf + (int64_t)v2 * R + g * 32 + lane) : INF;
+            }
+            __syncthreads();
+            const int32_t v = t * 32 + lane;
+            if (v < n)
+                for (int r = warp; r < 32; r += nwb) {
+                    const int32_t row = g * 32 + r;
+                    if (row < nrows) a.table[(int64_t)__ldg(a.rows + row) * a.ld + v] = tile[lane][r];
+                }
+            __syncthreads();
         }
-        __syncthreads();
-        const int32_t v = t * 32 + lane;
-        if (v < n)
-            for (int r = warp; r < nrows; r += nwb) a.table[(int64_t)__ldg(a.rows + r) * a.ld + v] = tile[lane][r];
-        __syncthreads();
     }
-}
-
-// Records a launch-level barrier error into the solve status.
-__global__ void k_collect_err(const uint32_t *ctrl, DevStat *stat)
-{
-    if (threadIdx.x == 0 && ctrl[C_ERR] != 0) atomicOr(&stat->err, ctrl[C_ERR]);
 }
 
 // ------------------------------------------------------------- traceback

@@ -32,7 +32,7 @@ constexpr int BATCH_CLASSES = 12;  // (n bucket 0..3) x (k bucket 0..2)
 struct emv_ctx {
     int device = 0;
     int sms = 0;
-    int relax_blocks_max = 0;
+    int relax_blocks_max[3] = {0, 0, 0};  // cooperative grid of k_relax<1>, <2>, <4>
     DevBuf ctrl, stat;             // relaxation barrier words, solve status
     DevBuf scratch, act;           // vertex-major chunk buffer, active flags
     DevBuf adj;                    // packed (col, w) arcs
@@ -45,6 +45,9 @@ struct emv_ctx {
     int32_t xs_k = -1;             // k of the cached subset list
     std::vector<uint32_t> xs_host;
     std::vector<int64_t> xs_off;   // level m occupies xs[off[m], off[m+1])
+    DevBuf mpairs, movr;           // merge pair slots and override slots, all levels of xs_k
+    std::vector<int64_t> mpair_base, movr_base;  // per level
+    bool merge_attr = false;
     int64_t launches = 0;
     // batched launch
     DevBuf bxs, bxs_off;           // subset lists of every k <= BATCH_KMAX

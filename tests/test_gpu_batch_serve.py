@@ -1,0 +1,113 @@
+"""Batched launch and continuous-batching server: every cost equals the
+single-instance solve (and the oracle), alone and in the mix."""
+import time
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def mixed(emv):
+    """80 instances of the mixed distribution (n log-uniform in [64, 4096],
+    degree {3,4,6,8}, k in [4, 10], about 10% group instances)."""
+    return [emv.Csr.from_stp(emv.StpInstance.mixed(777, i)) for i in range(80)]
+
+
+def test_batch_costs_equal_single_and_oracle(emv, orc, mixed):
+    with emv.Solver(0) as s:
+        costs, stats = s.batch_solve(mixed)
+        single = [s.solve(g).cost for g in mixed]
+    assert list(costs) == single
+    for g, c in zip(mixed[:24], costs[:24]):
+        _, want = orc.emv_table(g.n, g.row_ptr, g.col, g.w, g.terminals, threads=8)
+        assert c == want
+    assert stats["work_items"] == len(mixed) and stats["total_ms"] > 0
+
+
+def test_batch_repeat_and_autotune(emv, mixed):
+    with emv.Solver(0) as s:
+        a, _ = s.batch_solve(mixed)
+        b, _ = s.batch_solve(mixed)  # replays the captured graph
+        table = s.batch_autotune(mixed)
+        c, st = s.batch_solve(mixed)
+    assert np.array_equal(a, b) and np.array_equal(a, c)
+    assert set(int(x) for x in table) <= {0, 4, 8, 16, 32} and table.max() > 0
+
+
+def test_batch_group_instances(emv, orc):
+    groups = []
+    i = 0
+    while len(groups) < 6:
+        inst = emv.StpInstance.mixed(4242, i)
+        i += 1
+        if (inst.edges[:, 2] == 0).any():
+            groups.append(emv.Csr.from_stp(inst))
+    with emv.Solver(0) as s:
+        costs, _ = s.batch_solve(groups)
+    for g, c in zip(groups, costs):
+        _, want = orc.emv_table(g.n, g.row_ptr, g.col, g.w, g.terminals, threads=8)
+        assert c == want
+
+
+def test_batch_rejects_out_of_range(emv):
+    big_k = emv.Csr.from_stp(emv.StpInstance.regular(200, 4, 1, 10, 11, 1))
+    with emv.Solver(0) as s:
+        with pytest.raises(emv.EmvError) as ei:
+            s.batch_solve([big_k])
+        assert ei.value.status == 1
+
+
+def test_server_result_same_alone_and_in_mix(emv, mixed):
+    """Continuous batching: a request's cost is the same when it runs alone
+    and when it shares waves with 80 others plus a large request that runs on
+    the multi-CTA path concurrently."""
+    probe = mixed[5]
+    large = emv.Csr.from_stp(emv.StpInstance.regular(70000, 8, 1, 1000, 9, 99))
+    with emv.Solver(0) as s:
+        want = {i: s.solve(g).cost for i, g in enumerate(mixed)}
+        want_large = s.solve(large).cost
+    with emv.Server(0, hbm_budget_bytes=20 * 10**9, max_slots=256, large_n=65536) as srv:
+        rid = srv.submit(probe)
+        alone, _ = srv.wait(rid)
+        assert alone == want[5]
+        ids = {}
+        lid = srv.submit(large)
+        for i, g in enumerate(mixed):
+            ids[srv.submit(g)] = i
+            if i % 10 == 0:
+                time.sleep(0.002)  # arrivals while earlier requests are on the GPU
+        for r, i in ids.items():
+            cost, lat = srv.wait(r)
+            assert cost == want[i], i
+            assert lat >= 0
+        assert srv.wait(lid)[0] == want_large
+        st = srv.stats()
+    assert st["completed"] == len(mixed) + 2
+    assert st["peak_resident"] > 1 and st["waves"] >= 10
+
+
+def test_server_admission_budget_and_cancel(emv, mixed):
+    one = mixed[0]
+    need = (one.n << one.k) * 4
+    with emv.Server(0, hbm_budget_bytes=need // 2, max_slots=8) as srv:
+        with pytest.raises(emv.EmvError) as ei:
+            srv.submit(one)
+        assert ei.value.status == 4  # EMV_ERR_OVER_BUDGET
+        assert srv.stats()["rejected"] == 1
+    budget = 3 * max((g.n << g.k) * 4 + 64 * g.n for g in mixed[:20])
+    with emv.Server(0, hbm_budget_bytes=budget, max_slots=4) as srv:
+        ids = [srv.submit(g) for g in mixed[:20]]
+        srv.cancel(ids[-1])
+        done = 0
+        for r in ids[:-1]:
+            srv.wait(r)
+            done += 1
+        try:
+            srv.wait(ids[-1])  # finished before the cancel reached it
+        except emv.EmvError as e:
+            assert e.status == 10  # EMV_ERR_CANCELLED
+        assert done == 19
+        st = srv.stats()
+    assert st["peak_resident"] <= 4 and st["peak_bytes"] <= budget
