@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include "emv_common.cuh"
+#include "emv_device_util.cuh"
 
 namespace emv {
 
@@ -38,39 +39,6 @@ struct RelaxArgs {
     DevStat *stat;
     int32_t max_sweeps;
 };
-
-// Grid-wide barrier for a cooperative launch.  Bounded: a block that waits
-// longer than SPIN_LIMIT iterations, or sees another block's error, records
-// the error and returns false; every block then leaves the kernel.
-__device__ __forceinline__ bool grid_barrier(uint32_t *ctrl, int *s_ok)
-{
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile uint32_t *vc = ctrl;
-        const uint32_t gen = vc[C_BAR_GEN];
-        __threadfence();
-        const uint32_t arrived = atomicAdd(ctrl + C_BAR_COUNT, 1u);
-        if (arrived == gridDim.x - 1) {
-            atomicExch(ctrl + C_BAR_COUNT, 0u);
-            __threadfence();
-            atomicAdd(ctrl + C_BAR_GEN, 1u);
-        } else {
-            uint32_t spins = 0;
-            while (vc[C_BAR_GEN] == gen) {
-                if (vc[C_ERR] != 0) break;
-                if (++spins > SPIN_LIMIT) {
-                    atomicOr(ctrl + C_ERR, (uint32_t)EMV_DEV_BARRIER_TIMEOUT);
-                    break;
-                }
-                __nanosleep(256);
-            }
-        }
-        __threadfence();
-        *s_ok = (vc[C_ERR] == 0);
-    }
-    __syncthreads();
-    return *s_ok != 0;
-}
 
 __global__ void k_fill(int32_t *__restrict__ p, int64_t count, int32_t value)
 {
@@ -176,35 +144,6 @@ __global__ void __launch_bounds__(1024) k_merge_smem(int32_t *__restrict__ table
         }
     }
 }
-
-// Vector of VEC int32 (one lane's share of a vertex record).
-template <int VEC> struct IVec;
-template <> struct IVec<1> {
-    using T = int32_t;
-};
-template <> struct IVec<2> {
-    using T = int2;
-};
-template <> struct IVec<4> {
-    using T = int4;
-};
-
-__device__ __forceinline__ int32_t vmin(int32_t a, int32_t b) { return min(a, b); }
-__device__ __forceinline__ int2 vmin(int2 a, int2 b) { return make_int2(min(a.x, b.x), min(a.y, b.y)); }
-__device__ __forceinline__ int4 vmin(int4 a, int4 b)
-{
-    return make_int4(min(a.x, b.x), min(a.y, b.y), min(a.z, b.z), min(a.w, b.w));
-}
-__device__ __forceinline__ int32_t vadd(int32_t a, int32_t w) { return a + w; }
-__device__ __forceinline__ int2 vadd(int2 a, int32_t w) { return make_int2(a.x + w, a.y + w); }
-__device__ __forceinline__ int4 vadd(int4 a, int32_t w) { return make_int4(a.x + w, a.y + w, a.z + w, a.w + w); }
-__device__ __forceinline__ bool vlt(int32_t a, int32_t b) { return a < b; }
-__device__ __forceinline__ bool vlt(int2 a, int2 b) { return a.x < b.x || a.y < b.y; }
-__device__ __forceinline__ bool vlt(int4 a, int4 b) { return a.x < b.x || a.y < b.y || a.z < b.z || a.w < b.w; }
-template <typename T> __device__ __forceinline__ T vinf();
-template <> __device__ __forceinline__ int32_t vinf<int32_t>() { return INF; }
-template <> __device__ __forceinline__ int2 vinf<int2>() { return make_int2(INF, INF); }
-template <> __device__ __forceinline__ int4 vinf<int4>() { return make_int4(INF, INF, INF, INF); }
 
 // Multi-source shortest-path closure of up to 32*VEC rows (R:2109-2130): for
 // every row X of the chunk, d[X][v] = min over u of init[u] + dist(u, v).
