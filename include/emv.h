@@ -176,6 +176,27 @@ int emv_solve_dev(emv_ctx *ctx, const emv_graph *d_g, const int32_t *terminals,
 int emv_sssp(emv_ctx *ctx, const emv_graph *g, int32_t source,
              int64_t *dist_out, float *ms_out, void *stream);
 
+/* Shortest-path closure that allocates no device memory.  No counterpart in
+ * the reference.  For callers that cannot allocate device memory when they
+ * call in (another framework owns the device's memory through its own pool,
+ * a latency-critical loop must not pay cudaMalloc/cudaFree's device-wide
+ * synchronisation, or a host application forbids allocation after start-up):
+ * for r < rows, d_out[r*ld + v] = min over u of d_init[r*ld + u] + dist(u, v)
+ * on the device CSR (d_row_ptr, d_col, d_w), EMV_INF32 meaning "no value".
+ * Its working memory is one fixed device array of about 17 MiB inside the
+ * library, held on every GPU that loads the library until the process exits;
+ * limits: n <= 131072 vertices and rows <= 32 (larger sizes return
+ * EMV_ERR_BAD_INPUT).  It calls no allocator.  The first call on a device
+ * looks up that array's device address (set-up, done once per device with
+ * the device current); make that first call before any stream capture.
+ * Every call shares the array, so calls whose executions overlap on the GPU
+ * race: issue them on one stream or otherwise serialise them.  d_out may
+ * equal d_init.  Waits for the stream to read the completion status. */
+int emv_closure_noalloc(int32_t n, int64_t arcs, const int32_t *d_row_ptr,
+                        const int32_t *d_col, const int32_t *d_w,
+                        const int32_t *d_init, int32_t rows, int64_t ld,
+                        int32_t *d_out, void *stream);
+
 /* ------------------------------------------------------------- batching */
 
 typedef struct emv_instance {

@@ -117,6 +117,7 @@ SIGNATURES = {
     "emv_solve": (ctypes.c_int, [_P, ctypes.POINTER(_Graph), _P, _I32, _I32, ctypes.POINTER(_Result), _P]),
     "emv_solve_dev": (ctypes.c_int, [_P, ctypes.POINTER(_Graph), _P, _I32, _I32, ctypes.POINTER(_Result), _P]),
     "emv_sssp": (ctypes.c_int, [_P, ctypes.POINTER(_Graph), _I32, _P, ctypes.POINTER(ctypes.c_float), _P]),
+    "emv_closure_noalloc": (ctypes.c_int, [_I32, _I64, _P, _P, _P, _P, _I32, _I64, _P, _P]),
     "emv_batch_solve": (ctypes.c_int, [_P, ctypes.POINTER(_Instance), _I32, _P, ctypes.POINTER(_BatchStats), _P]),
     "emv_batch_autotune": (ctypes.c_int, [_P, ctypes.POINTER(_Instance), _I32, _P, _P]),
     "emv_batch_set_tuning": (ctypes.c_int, [_P, _P, _I32]),
@@ -377,6 +378,12 @@ class Solver:
     def batch_set_tuning(self, rcap) -> None:
         r = np.ascontiguousarray(rcap, dtype=np.int32)
         _check(self._lib.emv_batch_set_tuning(self._ctx, r.ctypes.data, int(r.shape[0])))
+
+    @staticmethod
+    def closure_noalloc(n: int, arcs: int, row_ptr: int, col: int, w: int, init: int, rows: int, ld: int,
+                        out: int, stream: Optional[int] = None) -> None:
+        """Shortest-path closure of up to 32 device rows with no device allocation (emv_closure_noalloc)."""
+        _check(load_library().emv_closure_noalloc(n, arcs, row_ptr, col, w, init, rows, ld, out, stream))
 
     def batch_solve(self, graphs: Sequence[Csr], stream: Optional[int] = None) -> tuple[np.ndarray, dict]:
         """Many independent instances in one persistent launch (emv_batch_solve)."""

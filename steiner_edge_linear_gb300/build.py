@@ -34,6 +34,7 @@ SOURCES = [
     "emv_device.cu",
     "emv_batch.cu",
     "emv_server.cpp",
+    "emv_noalloc.cu",
 ]
 CLI_SOURCES = ["cli.cpp"]
 
