@@ -308,6 +308,7 @@ def run_single(args, dist: Dist) -> dict:
            "gpu_launches": launches * args.steps,
            "phases_ms": {"merge": round(merge_ms, 3), "relax_incl_level1": round(relax_ms, 3),
                          "kernel": round(kernel_ms, 3)},
+           "relax_sweeps_per_solve": int(statistics.median(t["relax_sweeps"] for t in timings)),
            "gcell_per_s": round(((1 << k) * n) / (kernel_ms / 1000.0) / 1e9, 3),
            "merge_gbs_algorithmic": round(merge_bytes(n, k) / (merge_ms / 1000.0) / 1e9, 1),
            "relax_gbs_algorithmic": round(rows * relax_bytes_per_row(n, m) / (relax_ms / 1000.0) / 1e9, 1),

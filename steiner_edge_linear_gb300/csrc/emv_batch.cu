@@ -197,6 +197,7 @@ int batch_pack(emv_ctx *c, const emv_instance *inst, const std::vector<int32_t> 
         terms += I.k;
         words += ((int64_t)I.g.n << I.k);
         pk.rcap_used = std::max(pk.rcap_used, d.rcap);
+        pk.cost_slots = std::max<int64_t>(pk.cost_slots, (int64_t)d.orig + 1);
     }
     pk.rows = rows;
     pk.arcs = arcs;
@@ -243,12 +244,15 @@ int batch_upload(emv_ctx *c, BatchPack &pk, cudaStream_t st)
     if (!r) r = dev_reserve(c->b_term, sizeof(int32_t) * (size_t)std::max<int64_t>(pk.terms, 1));
     if (!r) r = dev_reserve(c->b_desc, sizeof(BatchInst) * (size_t)pk.count);
     if (!r) r = dev_reserve(c->b_table, sizeof(int32_t) * (size_t)pk.table_words);
-    if (!r) r = dev_reserve(c->b_costs, sizeof(int64_t) * (size_t)pk.count);
+    // costs are written at index orig (the caller's instance index), which can
+    // exceed the number of instances in this launch when it is a sample
+    if (!r) r = dev_reserve(c->b_costs, sizeof(int64_t) * (size_t)std::max<int64_t>(pk.cost_slots, 1));
     if (!r) r = dev_reserve(c->b_ctrl, 64);
     if (!r) r = prepare_batch_subsets(c, st);
     if (r) return r;
     for (int32_t j = 0; j < pk.count; j++) {
         BatchInst &d = pk.h_desc[j];
+        if (d.orig < 0 || d.orig >= pk.cost_slots) return emv_fail(EMV_ERR_INTERNAL, "batch: cost slot out of range");
         d.row_ptr = (const int32_t *)c->b_row.ptr + pk.row_off[(size_t)j];
         d.adj = (const int2 *)c->b_adj.ptr + pk.arc_off[(size_t)j];
         d.terms = (const int32_t *)c->b_term.ptr + pk.term_off[(size_t)j];

@@ -13,6 +13,7 @@ struct BatchPack {
     int64_t rows = 0, arcs = 0, terms = 0, table_words = 0;
     int32_t count = 0;
     int32_t rcap_used = 0;
+    int64_t cost_slots = 0;            // entries the device cost array needs (max orig + 1)
     int32_t *h_row = nullptr;          // views into the pinned staging buffer
     int2 *h_adj = nullptr;
     int32_t *h_term = nullptr;

@@ -151,8 +151,8 @@ int launch_relax(emv_ctx *c, const int32_t *row_ptr, const int2 *adj, int32_t n,
     a.max_sweeps = n + 1;
     const int vi = nrows <= 32 ? 0 : nrows <= 64 ? 1 : 2;
     const void *fn = vi == 0 ? (const void *)k_relax<1> : vi == 1 ? (const void *)k_relax<2> : (const void *)k_relax<4>;
-    // A warp per 32 vertices is enough; small graphs use fewer blocks (cheaper barriers).
-    const int vpb = 32 * (RELAX_THREADS / 32);
+    // A warp per 8 vertices is enough; small graphs use fewer blocks (cheaper barriers).
+    const int vpb = 8 * (RELAX_THREADS / 32);
     const int blocks = std::min(c->relax_blocks_max[vi], std::max(1, (n + vpb - 1) / vpb));
     CUDA_TRY(cudaMemsetAsync(a.ctrl, 0, sizeof(uint32_t) * C_WORDS, st));
     void *args[] = {&a};

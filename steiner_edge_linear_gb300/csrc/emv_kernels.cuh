@@ -107,6 +107,7 @@ __global__ void __launch_bounds__(1024) k_merge_smem(int32_t *__restrict__ table
                                                      const int32_t *__restrict__ terms)
 {
     extern __shared__ int32_t S[];
+    __shared__ uint32_t red[32 * 32];  // per-subset partial minima when warps share a subset
     constexpr int G = 32 / VB;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int32_t v0 = blockIdx.x * VB;
@@ -115,15 +116,22 @@ __global__ void __launch_bounds__(1024) k_merge_smem(int32_t *__restrict__ table
         const int32_t v = v0 + j;
         S[idx] = (v < n) ? __ldg(table + (int64_t)__ldg(stage_rows + i) * ld + v) : INF;
     }
+    // Few subsets (the top levels): split each subset's pairs over `parts` warps.
+    const int parts = cnt >= nw ? 1 : nw / cnt;
+    if (parts > 1)
+        for (int i = threadIdx.x; i < cnt * VB; i += blockDim.x) red[i] = (uint32_t)INF;
     __syncthreads();
     const int slice = lane / VB, j = lane % VB;
     const int32_t v = v0 + j;
-    for (int32_t xi = warp; xi < cnt; xi += nw) {
+    const int32_t tasks = cnt * parts;
+    for (int32_t t = warp; t < tasks; t += nw) {
+        const int32_t xi = t / parts, part = t - xi * parts;
         const uint32_t *P = pairs + (int64_t)xi * npairs;
+        const int32_t step = G * parts;
         uint32_t acc = (uint32_t)INF, acc2 = (uint32_t)INF;
-        int32_t p = slice;
-        for (; p + G < npairs; p += 2 * G) {
-            const uint32_t q0 = __ldg(P + p), q1 = __ldg(P + p + G);
+        int32_t p = part * G + slice;
+        for (; p + step < npairs; p += 2 * step) {
+            const uint32_t q0 = __ldg(P + p), q1 = __ldg(P + p + step);
             acc = min(acc, (uint32_t)S[(q0 & 0xffffu) * VB + j] + (uint32_t)S[(q0 >> 16) * VB + j]);
             acc2 = min(acc2, (uint32_t)S[(q1 & 0xffffu) * VB + j] + (uint32_t)S[(q1 >> 16) * VB + j]);
         }
@@ -134,7 +142,24 @@ __global__ void __launch_bounds__(1024) k_merge_smem(int32_t *__restrict__ table
         acc = min(acc, acc2);
 #pragma unroll
         for (int off = 16; off >= VB; off >>= 1) acc = min(acc, __shfl_xor_sync(FULL, acc, off));
+        if (parts > 1) {
+            if (slice == 0) atomicMin(&red[xi * VB + j], acc);
+            continue;
+        }
         if (slice == 0 && v < n) {
+            const uint32_t *O = ovr + (int64_t)xi * m;
+            for (int i = 0; i < m; i++) {
+                const uint32_t o = __ldg(O + i);
+                if (__ldg(terms + (o >> 16)) == v) acc = (uint32_t)S[(o & 0xffffu) * VB + j];
+            }
+            table[(int64_t)__ldg(xs_level + xi) * ld + v] = (int32_t)acc;
+        }
+    }
+    if (parts > 1) {
+        __syncthreads();
+        for (int32_t xi = warp; xi < cnt; xi += nw) {
+            if (slice != 0 || v >= n) continue;
+            uint32_t acc = red[xi * VB + j];
             const uint32_t *O = ovr + (int64_t)xi * m;
             for (int i = 0; i < m; i++) {
                 const uint32_t o = __ldg(O + i);
@@ -151,8 +176,8 @@ __global__ void __launch_bounds__(1024) k_merge_smem(int32_t *__restrict__ table
 //   A. transpose the rows into a vertex-major buffer: vertex v owns one
 //      record of R = 32*VEC int32 (lane l holds rows l*VEC .. l*VEC+VEC-1);
 //      in level-1 mode the rows are the k single-source initialisations;
-//   B. frontier sweeps: a warp takes 32 vertices at once, reads their active
-//      flags and CSR bounds with one coalesced load each, and for every
+//   B. frontier sweeps: a warp takes 8 vertices at once, reads their active
+//      flags and CSR bounds with one load each, and for every
 //      active vertex pulls min over its arcs (u, w) of rec[u] + w -- one
 //      coalesced 128*VEC-byte gather per arc, 2 KB in flight per warp -- and writes
 //      the record in place.  Only the owner writes a record and values only
@@ -167,6 +192,7 @@ __global__ void __launch_bounds__(RELAX_THREADS, 2) k_relax(RelaxArgs a)
     using V = typename IVec<VEC>::T;
     constexpr int R = 32 * VEC;
     constexpr int GROUP = VEC == 4 ? 4 : 8;  // gathers in flight per warp: 2 KB for VEC >= 2
+    constexpr int TASK_V = 8;                  // vertices per warp task
     __shared__ int32_t tile[32][33];
     __shared__ int s_ok;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwb = blockDim.x >> 5;
@@ -208,9 +234,10 @@ __global__ void __launch_bounds__(RELAX_THREADS, 2) k_relax(RelaxArgs a)
         return;
     }
 
-    // ---- B: frontier sweeps
+    // ---- B: frontier sweeps (a warp task is TASK_V consecutive vertices)
     const int32_t gw = (int32_t)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int32_t nwg = (int32_t)((gridDim.x * blockDim.x) >> 5);
+    const int32_t ntasks = (n + TASK_V - 1) / TASK_V;
     volatile uint32_t *vctrl = a.ctrl;
     const V *recs = reinterpret_cast<const V *>(buf);
     int32_t s = 0;
@@ -220,18 +247,18 @@ __global__ void __launch_bounds__(RELAX_THREADS, 2) k_relax(RelaxArgs a)
         uint8_t *nxt = (s & 1) ? a.act0 : a.act1;
         if (blockIdx.x == 0 && threadIdx.x == 0) vctrl[C_SLOT0 + (s + 1) % 3] = 0;
         bool any = false;
-        for (int32_t blk = gw; blk < ntiles; blk += nwg) {
-            const int32_t v = blk * 32 + lane;
-            const bool f = v < n && __ldcg(cur + v) != 0;
+        for (int32_t blk = gw; blk < ntasks; blk += nwg) {
+            const int32_t v = blk * TASK_V + lane;
+            const bool f = lane < TASK_V && v < n && __ldcg(cur + v) != 0;
             unsigned act = __ballot_sync(FULL, f);
             if (!act) continue;
             if (f) cur[v] = 0;
-            const int32_t rp0 = v < n ? __ldg(a.row_ptr + v) : 0;
-            const int32_t rp1 = v < n ? __ldg(a.row_ptr + v + 1) : 0;
+            const int32_t rp0 = (lane < TASK_V && v < n) ? __ldg(a.row_ptr + v) : 0;
+            const int32_t rp1 = (lane < TASK_V && v < n) ? __ldg(a.row_ptr + v + 1) : 0;
             while (act) {
                 const int j = __ffs(act) - 1;
                 act &= act - 1;
-                const int32_t vv = blk * 32 + j;
+                const int32_t vv = blk * TASK_V + j;
                 const int32_t beg = __shfl_sync(FULL, rp0, j), end = __shfl_sync(FULL, rp1, j);
                 V *mine = reinterpret_cast<V *>(buf + (int64_t)vv * R) + lane;
                 const V old = __ldcg(mine);

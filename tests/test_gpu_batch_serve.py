@@ -111,3 +111,16 @@ def test_server_admission_budget_and_cancel(emv, mixed):
         assert done == 19
         st = srv.stats()
     assert st["peak_resident"] <= 4 and st["peak_bytes"] <= budget
+
+
+def test_autotune_first_on_fresh_context(emv):
+    """Autotune samples instances by class; their cost slots are the callers'
+    indices, which can exceed the sample size (a fresh context has no larger
+    cost buffer from an earlier batch)."""
+    graphs = [emv.Csr.from_stp(emv.StpInstance.mixed(31, i)) for i in range(300)]
+    with emv.Solver(0) as s:
+        table = s.batch_autotune(graphs)
+        costs, _ = s.batch_solve(graphs)
+        ref = [s.solve(g).cost for g in graphs[::25]]
+    assert table.max() > 0
+    assert list(costs[::25]) == ref
