@@ -110,7 +110,8 @@ extern "C" int emv_destroy(emv_ctx *c)
     if (!c) return EMV_OK;
     cudaSetDevice(c->device);
     cudaDeviceSynchronize();
-    for (DevBuf *b : {&c->ctrl, &c->stat, &c->scratch, &c->act, &c->adj, &c->xs, &c->mpairs, &c->movr, &c->terms, &c->g_row,
+    for (DevBuf *b : {&c->ctrl, &c->stat, &c->scratch, &c->act, &c->adj, &c->xs, &c->mpairs, &c->movr,
+                      &c->mstream_data, &c->mstream_phases, &c->terms, &c->g_row,
                       &c->g_col, &c->g_w, &c->table, &c->tb_edges, &c->tb_out, &c->tb_work})
         dev_release(*b);
     for (int i = 0; i < MAX_EVENTS; i++)
@@ -172,6 +173,108 @@ int reserve_relax(emv_ctx *c, int32_t n)
 constexpr int32_t MERGE_SMEM_BYTES = 220 * 1024;
 constexpr int32_t MERGE_SMEM_KMAX = 15;  // staged slots must fit 16 bits
 
+constexpr int32_t STREAM_SMEM_BYTES = 224 * 1024;
+
+// Plan of the streamed merge (k_merge_stream) for every level of k: phases
+// j = 1..m/2 staging the rows of sizes j and m-j, with each subset's pairs as
+// staged positions.  A level whose accumulators plus largest phase exceed the
+// shared memory keeps the staged-all-lower-rows kernel.
+int plan_stream_merge(emv_ctx *c, int32_t k, cudaStream_t st)
+{
+    const std::vector<uint32_t> &xs = c->xs_host;
+    const std::vector<int64_t> &off = c->xs_off;
+    c->mstream_phase_off.assign((size_t)k + 2, 0);
+    c->mstream_nphase.assign((size_t)k + 2, 0);
+    c->mstream_smem.assign((size_t)k + 2, 0);
+    if (k > MERGE_SMEM_KMAX) return EMV_OK;
+    std::vector<uint32_t> rank((size_t)1 << k, 0);  // position within its level
+    for (int32_t m = 1; m <= k; m++)
+        for (int64_t i = off[(size_t)m]; i < off[(size_t)m + 1]; i++) rank[xs[(size_t)i]] = (uint32_t)(i - off[(size_t)m]);
+    struct HostPhase {
+        size_t rows_at, pairs_at;
+        int32_t nrows, npairs;
+    };
+    std::vector<uint32_t> data;
+    std::vector<std::vector<HostPhase>> plan((size_t)k + 2);
+    for (int32_t m = 2; m <= k; m++) {
+        const int64_t cnt = off[(size_t)m + 1] - off[(size_t)m];
+        const int64_t acc_bytes = cnt * 128;
+        int64_t worst = 0;
+        for (int32_t j = 1; 2 * j <= m; j++) {
+            const int64_t ny = off[(size_t)j + 1] - off[(size_t)j], nz = off[(size_t)(m - j) + 1] - off[(size_t)(m - j)];
+            const int64_t nrows = (j == m - j) ? ny : ny + nz;
+            worst = std::max(worst, (nrows + 1) * 128);
+        }
+        if (acc_bytes + worst > STREAM_SMEM_BYTES) continue;  // not streamed
+        for (int32_t j = 1; 2 * j <= m; j++) {
+            const bool same = (j == m - j);
+            const int64_t yb = off[(size_t)j], ny = off[(size_t)j + 1] - yb;
+            const int64_t zb = off[(size_t)(m - j)], nz = off[(size_t)(m - j) + 1] - zb;
+            HostPhase hp;
+            hp.rows_at = data.size();
+            for (int64_t i = 0; i < ny; i++) data.push_back(xs[(size_t)(yb + i)]);
+            if (!same)
+                for (int64_t i = 0; i < nz; i++) data.push_back(xs[(size_t)(zb + i)]);
+            hp.nrows = (int32_t)(same ? ny : ny + nz);
+            const uint32_t zoff = same ? 0 : (uint32_t)ny, pad = (uint32_t)hp.nrows;
+            // pairs of this phase per subset: all j-subsets Y of X (Y holding X's
+            // lowest terminal when both halves have the same size)
+            int32_t npairs = 0;
+            {
+                int64_t c_mj = 1;
+                for (int32_t i = 0; i < j; i++) c_mj = c_mj * (m - i) / (i + 1);
+                npairs = (int32_t)(same ? c_mj / 2 : c_mj);
+            }
+            hp.npairs = (npairs + 3) & ~3;
+            while (data.size() % 4) data.push_back(0);  // pairs are read as uint4: 16-byte aligned blocks
+            hp.pairs_at = data.size();
+            for (int64_t xi = 0; xi < cnt; xi++) {
+                const uint32_t X = xs[(size_t)(off[(size_t)m] + xi)];
+                const uint32_t low = X & (0u - X);
+                int32_t got = 0;
+                for (uint32_t Y = (X - 1) & X; Y; Y = (Y - 1) & X) {
+                    if (__builtin_popcount(Y) != j) continue;
+                    if (same && !(Y & low)) continue;
+                    data.push_back(rank[Y] | ((zoff + rank[X ^ Y]) << 16));
+                    got++;
+                }
+                if (got != npairs) return emv_fail(EMV_ERR_INTERNAL, "merge plan: %d pairs, expected %d", got, npairs);
+                for (; got < hp.npairs; got++) data.push_back(pad | (pad << 16));
+            }
+            plan[(size_t)m].push_back(hp);
+        }
+        c->mstream_smem[(size_t)m] = acc_bytes + worst;
+    }
+    if (data.empty()) return EMV_OK;
+    int r = dev_reserve(c->mstream_data, sizeof(uint32_t) * data.size());
+    if (r) return r;
+    std::vector<MergePhase> phases;
+    const uint32_t *base = (const uint32_t *)c->mstream_data.ptr;
+    for (int32_t m = 2; m <= k; m++) {
+        c->mstream_phase_off[(size_t)m] = (int64_t)phases.size();
+        c->mstream_nphase[(size_t)m] = (int64_t)plan[(size_t)m].size();
+        for (const HostPhase &hp : plan[(size_t)m]) {
+            if (hp.pairs_at % 4 != 0 || hp.npairs % 4 != 0)
+                return emv_fail(EMV_ERR_INTERNAL, "merge plan: pair block not 16-byte aligned");
+            MergePhase mp;
+            mp.rows = base + hp.rows_at;
+            mp.pairs = base + hp.pairs_at;
+            mp.nrows = hp.nrows;
+            mp.npairs = hp.npairs;
+            phases.push_back(mp);
+        }
+    }
+    r = dev_reserve(c->mstream_phases, sizeof(MergePhase) * std::max<size_t>(1, phases.size()));
+    if (r) return r;
+    CUDA_TRY(cudaMemcpyAsync(c->mstream_data.ptr, data.data(), sizeof(uint32_t) * data.size(), cudaMemcpyHostToDevice,
+                             st));
+    if (!phases.empty())
+        CUDA_TRY(cudaMemcpyAsync(c->mstream_phases.ptr, phases.data(), sizeof(MergePhase) * phases.size(),
+                                 cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return EMV_OK;
+}
+
 int prepare_subsets(emv_ctx *c, int32_t k, cudaStream_t st)
 {
     if (c->xs_k == k) return EMV_OK;
@@ -204,6 +307,8 @@ int prepare_subsets(emv_ctx *c, int32_t k, cudaStream_t st)
             }
         }
     }
+    r = plan_stream_merge(c, k, st);
+    if (r) return r;
     if (!pairs.empty()) {
         r = dev_reserve(c->mpairs, sizeof(uint32_t) * pairs.size());
         if (!r) r = dev_reserve(c->movr, sizeof(uint32_t) * ovr.size());
@@ -244,12 +349,21 @@ int launch_merge(emv_ctx *c, int32_t *table, int64_t ld, int32_t n, int32_t k, i
                               (const void *)k_merge_smem<2>, (const void *)k_merge_smem<1>};
         for (const void *f : fns)
             CUDA_TRY(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, MERGE_SMEM_BYTES));
+        CUDA_TRY(cudaFuncSetAttribute((const void *)k_merge_stream, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      STREAM_SMEM_BYTES));
         c->merge_attr = true;
     }
     const int64_t nstage = c->xs_off[(size_t)m];
     cudaError_t e = cudaSuccess;
     c->launches++;
-    if (k <= MERGE_SMEM_KMAX) {
+    if (k <= MERGE_SMEM_KMAX && c->mstream_smem[(size_t)m] > 0) {
+        const int64_t b = c->xs_off[(size_t)m], cnt = c->xs_off[(size_t)m + 1] - b;
+        k_merge_stream<<<(unsigned)((n + 31) / 32), 1024, (size_t)c->mstream_smem[(size_t)m], st>>>(
+            table, ld, n, (const uint32_t *)c->xs.ptr + b, (int32_t)cnt,
+            (const MergePhase *)c->mstream_phases.ptr + c->mstream_phase_off[(size_t)m],
+            (int32_t)c->mstream_nphase[(size_t)m], d_terms, k);
+        e = cudaGetLastError();
+    } else if (k <= MERGE_SMEM_KMAX) {
         const int64_t row_bytes = nstage * 4;
         if (row_bytes * 32 <= MERGE_SMEM_BYTES) e = merge_smem_launch<32>(c, table, ld, n, k, m, d_terms, st);
         else if (row_bytes * 16 <= MERGE_SMEM_BYTES) e = merge_smem_launch<16>(c, table, ld, n, k, m, d_terms, st);

@@ -170,6 +170,85 @@ __global__ void __launch_bounds__(1024) k_merge_smem(int32_t *__restrict__ table
     }
 }
 
+// One phase of the streamed merge: the rows of sizes j and m-j staged
+// together, and for every subset X of level m the pairs {Y, X\Y} with
+// |Y| = j as staged positions (posY | posZ << 16), padded with (pad, pad)
+// to a multiple of 4 (pad = nrows, a staged row of INF).
+struct MergePhase {
+    const uint32_t *rows;   // staged subsets, level order
+    const uint32_t *pairs;  // [cnt][npairs]
+    int32_t nrows;
+    int32_t npairs;         // per subset, multiple of 4
+};
+
+// Streamed subset merge of level m (R:2068-2107) with a lane per vertex at
+// every level.  Block = 32 consecutive vertices; the minima of all C(k,m)
+// subsets live in shared memory (acc) while the phases j = 1..m/2 stage only
+// the rows of sizes j and m-j; lanes read consecutive words of a staged row,
+// so the pair loop is free of bank conflicts.
+// Subsets with few pairs per warp (the top levels) split their list over
+// several warps; partial minima meet in acc through shared-memory atomicMin.
+// The terminal override of the virtual-source arcs (R:2099-2107) is applied
+// last, from the finished level m-1 rows in the table.
+__global__ void __launch_bounds__(1024) k_merge_stream(int32_t *__restrict__ table, int64_t ld, int32_t n,
+                                                       const uint32_t *__restrict__ xs_level, int32_t cnt,
+                                                       const MergePhase *__restrict__ phases, int32_t nphase,
+                                                       const int32_t *__restrict__ terms, int32_t k)
+{
+    extern __shared__ uint32_t sm[];
+    uint32_t *acc = sm;
+    uint32_t *S = sm + (size_t)cnt * 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int32_t v0 = blockIdx.x * 32, v = v0 + lane;
+    for (int32_t i = threadIdx.x; i < cnt * 32; i += blockDim.x) acc[i] = (uint32_t)INF;
+    const int parts = cnt >= nw ? 1 : nw / cnt;
+    for (int32_t ph = 0; ph < nphase; ph++) {
+        const MergePhase P = phases[ph];
+        __syncthreads();
+        for (int32_t i = warp; i <= P.nrows; i += nw)
+            S[i * 32 + lane] = (i < P.nrows && v < n) ? (uint32_t)__ldg(table + (int64_t)__ldg(P.rows + i) * ld + v)
+                                                      : (uint32_t)INF;
+        __syncthreads();
+        const int32_t quads = P.npairs >> 2;
+        const uint32_t *Sl = S + lane;
+        for (int32_t t = warp; t < cnt * parts; t += nw) {
+            const int32_t xi = t / parts, part = t - xi * parts;
+            const uint4 *Q = reinterpret_cast<const uint4 *>(P.pairs + (int64_t)xi * P.npairs);
+            uint32_t a0 = (uint32_t)INF, a1 = (uint32_t)INF;
+            int32_t qi = part;
+            uint4 q = qi < quads ? __ldg(Q + qi) : make_uint4(0, 0, 0, 0);
+            while (qi < quads) {
+                const int32_t qn = qi + parts;
+                const uint4 nq = qn < quads ? __ldg(Q + qn) : q;  // next quad in flight
+                a0 = min(a0, Sl[(q.x & 0xffffu) * 32] + Sl[(q.x >> 16) * 32]);
+                a1 = min(a1, Sl[(q.y & 0xffffu) * 32] + Sl[(q.y >> 16) * 32]);
+                a0 = min(a0, Sl[(q.z & 0xffffu) * 32] + Sl[(q.z >> 16) * 32]);
+                a1 = min(a1, Sl[(q.w & 0xffffu) * 32] + Sl[(q.w >> 16) * 32]);
+                q = nq;
+                qi = qn;
+            }
+            atomicMin(acc + xi * 32 + lane, min(a0, a1));
+        }
+    }
+    __syncthreads();
+    bool has_term = false;
+    for (int t = 0; t < k; t++) {
+        const int32_t tv = __ldg(terms + t);
+        has_term |= (tv >= v0 && tv < v0 + 32);
+    }
+    if (v >= n) return;
+    for (int32_t xi = warp; xi < cnt; xi += nw) {
+        const uint32_t X = __ldg(xs_level + xi);
+        uint32_t a = acc[xi * 32 + lane];
+        if (has_term)
+            for (uint32_t bits = X; bits; bits &= bits - 1) {
+                const int t = __ffs(bits) - 1;
+                if (__ldg(terms + t) == v) a = (uint32_t)table[(int64_t)(X ^ (1u << t)) * ld + v];
+            }
+        table[(int64_t)X * ld + v] = (int32_t)a;
+    }
+}
+
 // Multi-source shortest-path closure of up to 32*VEC rows (R:2109-2130): for
 // every row X of the chunk, d[X][v] = min over u of init[u] + dist(u, v).
 // One cooperative persistent launch:

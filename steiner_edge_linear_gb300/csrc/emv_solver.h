@@ -48,6 +48,9 @@ struct emv_ctx {
     DevBuf mpairs, movr;           // merge pair slots and override slots, all levels of xs_k
     std::vector<int64_t> mpair_base, movr_base;  // per level
     bool merge_attr = false;
+    // streamed merge plan of xs_k: per level, its phases (device) and smem bytes (0 = not streamed)
+    DevBuf mstream_data, mstream_phases;
+    std::vector<int64_t> mstream_phase_off, mstream_nphase, mstream_smem;
     int64_t launches = 0;
     // batched launch
     DevBuf bxs, bxs_off;           // subset lists of every k <= BATCH_KMAX
