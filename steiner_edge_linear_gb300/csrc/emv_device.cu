@@ -111,7 +111,7 @@ extern "C" int emv_destroy(emv_ctx *c)
     cudaSetDevice(c->device);
     cudaDeviceSynchronize();
     for (DevBuf *b : {&c->ctrl, &c->stat, &c->scratch, &c->act, &c->adj, &c->xs, &c->mpairs, &c->movr,
-                      &c->mstream_data, &c->mstream_phases, &c->terms, &c->g_row,
+                      &c->mstream_data, &c->mstream_phases, &c->stamp, &c->terms, &c->g_row,
                       &c->g_col, &c->g_w, &c->table, &c->tb_edges, &c->tb_out, &c->tb_work})
         dev_release(*b);
     for (int i = 0; i < MAX_EVENTS; i++)
@@ -135,6 +135,7 @@ int launch_relax(emv_ctx *c, const int32_t *row_ptr, const int2 *adj, int32_t n,
                  const uint32_t *rows, int32_t nrows, const int32_t *terms, int32_t level1, cudaStream_t st)
 {
     RelaxArgs a;
+    a.stamp = (int32_t *)c->stamp.ptr;
     a.row_ptr = row_ptr;
     a.adj = adj;
     a.n = n;
@@ -167,6 +168,7 @@ int reserve_relax(emv_ctx *c, int32_t n)
     const size_t npad = ((size_t)n + 31) / 32 * 32;
     int st = dev_reserve(c->scratch, npad * CHUNK_ROWS * sizeof(int32_t));
     if (!st) st = dev_reserve(c->act, 2 * (((size_t)n + 255) / 256 * 256));
+    if (!st) st = dev_reserve(c->stamp, sizeof(int32_t) * (size_t)n);
     return st;
 }
 

@@ -38,6 +38,7 @@ struct RelaxArgs {
     uint32_t *ctrl;         // C_WORDS words
     DevStat *stat;
     int32_t max_sweeps;
+    int32_t *stamp;         // n: last sweep in which the vertex changed (-1 none)
 };
 
 __global__ void k_fill(int32_t *__restrict__ p, int64_t count, int32_t value)
@@ -216,16 +217,20 @@ __global__ void __launch_bounds__(1024) k_merge_stream(int32_t *__restrict__ tab
             const uint4 *Q = reinterpret_cast<const uint4 *>(P.pairs + (int64_t)xi * P.npairs);
             uint32_t a0 = (uint32_t)INF, a1 = (uint32_t)INF;
             int32_t qi = part;
-            uint4 q = qi < quads ? __ldg(Q + qi) : make_uint4(0, 0, 0, 0);
+            // two quads of pairs in flight ahead of the one being reduced
+            const uint4 zq = make_uint4(0, 0, 0, 0);
+            uint4 q = qi < quads ? __ldg(Q + qi) : zq;
+            uint4 q1 = qi + parts < quads ? __ldg(Q + qi + parts) : zq;
             while (qi < quads) {
-                const int32_t qn = qi + parts;
-                const uint4 nq = qn < quads ? __ldg(Q + qn) : q;  // next quad in flight
+                const int32_t q2i = qi + 2 * parts;
+                const uint4 q2 = q2i < quads ? __ldg(Q + q2i) : zq;
                 a0 = min(a0, Sl[(q.x & 0xffffu) * 32] + Sl[(q.x >> 16) * 32]);
                 a1 = min(a1, Sl[(q.y & 0xffffu) * 32] + Sl[(q.y >> 16) * 32]);
                 a0 = min(a0, Sl[(q.z & 0xffffu) * 32] + Sl[(q.z >> 16) * 32]);
                 a1 = min(a1, Sl[(q.w & 0xffffu) * 32] + Sl[(q.w >> 16) * 32]);
-                q = nq;
-                qi = qn;
+                q = q1;
+                q1 = q2;
+                qi += parts;
             }
             atomicMin(acc + xi * 32 + lane, min(a0, a1));
         }
@@ -249,36 +254,141 @@ __global__ void __launch_bounds__(1024) k_merge_stream(int32_t *__restrict__ tab
     }
 }
 
+// Frontier sweeps over one chunk (phase B of k_relax).  A warp takes TASK_V
+// vertices, reads their active flags and CSR bounds with one load each, and
+// for every active vertex pulls min over its arcs (u, w) of rec[u] + w with
+// coalesced 128*VEC-byte gathers -- only from heads stamped as changed in the
+// previous sweep (a head that last changed earlier was already pulled when
+// that change marked this vertex active).  The arcs and stamps of the next
+// active vertex are loaded while the current one's gathers are in flight.
+// Only the owner writes a record and values only decrease, so no atomics are
+// needed.  Returns the number of sweeps, or -1 after an error (recorded).
+template <int VEC>
+__device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
+{
+    using V = typename IVec<VEC>::T;
+    constexpr int GROUP = VEC == 4 ? 4 : 8;  // gathers in flight per group (2 KB for VEC >= 2)
+    constexpr int TASK_V = 8;
+    const int lane = threadIdx.x & 31;
+    const int32_t n = a.n;
+    const int32_t gw = (int32_t)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int32_t nwg = (int32_t)((gridDim.x * blockDim.x) >> 5);
+    const int32_t ntasks = (n + TASK_V - 1) / TASK_V;
+    volatile uint32_t *vctrl = a.ctrl;
+    const V *recs = reinterpret_cast<const V *>(a.scratch);  // vertex v: recs[v * 32 .. v * 32 + 31]
+    int32_t s = 0;
+    for (; s < a.max_sweeps; s++) {
+        uint8_t *cur = (s & 1) ? a.act1 : a.act0;
+        uint8_t *nxt = (s & 1) ? a.act0 : a.act1;
+        if (blockIdx.x == 0 && threadIdx.x == 0) vctrl[C_SLOT0 + (s + 1) % 3] = 0;
+        bool any = false;
+        for (int32_t blk = gw; blk < ntasks; blk += nwg) {
+            const int32_t v = blk * TASK_V + lane;
+            const bool f = lane < TASK_V && v < n && __ldcg(cur + v) != 0;
+            unsigned act = __ballot_sync(FULL, f);
+            if (!act) continue;
+            if (f) cur[v] = 0;
+            const int32_t rp0 = (lane < TASK_V && v < n) ? __ldg(a.row_ptr + v) : 0;
+            const int32_t rp1 = (lane < TASK_V && v < n) ? __ldg(a.row_ptr + v + 1) : 0;
+            // first active vertex: bounds, first 32 arcs and their selection
+            int j = __ffs(act) - 1;
+            act &= act - 1;
+            int32_t beg = __shfl_sync(FULL, rp0, j), end = __shfl_sync(FULL, rp1, j);
+            int2 arc = make_int2(0, 0);
+            bool pull = false;
+            if (beg + lane < end) {
+                arc = __ldg(a.adj + beg + lane);
+                pull = s == 0 || __ldcg(a.stamp + arc.x) >= s - 1;
+            }
+            for (;;) {
+                const int32_t vv = blk * TASK_V + j;
+                V *mine = reinterpret_cast<V *>(a.scratch + (int64_t)vv * 32 * VEC) + lane;
+                const V old = __ldcg(mine);
+                V acc = old;
+                for (int32_t e0 = beg;;) {
+                    unsigned sel = __ballot_sync(FULL, pull);
+                    while (sel) {
+                        V val[GROUP];
+                        int32_t wt[GROUP];
+                        bool ok[GROUP];
+#pragma unroll
+                        for (int g = 0; g < GROUP; g++) {
+                            ok[g] = sel != 0;
+                            const int src = ok[g] ? __ffs(sel) - 1 : 0;
+                            sel &= sel - 1;
+                            const int32_t u = __shfl_sync(FULL, arc.x, src);
+                            wt[g] = __shfl_sync(FULL, arc.y, src);
+                            val[g] = ok[g] ? __ldcg(recs + (int64_t)u * 32 + lane) : vinf<V>();
+                        }
+#pragma unroll
+                        for (int g = 0; g < GROUP; g++) acc = vmin(acc, vadd(val[g], wt[g]));
+                    }
+                    e0 += 32;
+                    if (e0 >= end) break;
+                    pull = false;  // high-degree vertex: next 32 arcs
+                    if (e0 + lane < end) {
+                        arc = __ldg(a.adj + e0 + lane);
+                        pull = s == 0 || __ldcg(a.stamp + arc.x) >= s - 1;
+                    }
+                }
+                // prefetch the next active vertex before finishing this one
+                const int32_t cbeg = beg, cend = end;
+                const bool more = act != 0;
+                if (more) {
+                    j = __ffs(act) - 1;
+                    act &= act - 1;
+                    beg = __shfl_sync(FULL, rp0, j);
+                    end = __shfl_sync(FULL, rp1, j);
+                    pull = false;
+                    arc = make_int2(0, 0);
+                    if (beg + lane < end) {
+                        arc = __ldg(a.adj + beg + lane);
+                        pull = s == 0 || __ldcg(a.stamp + arc.x) >= s - 1;
+                    }
+                }
+                const bool dec = vlt(acc, old);
+                if (dec) __stcg(mine, acc);
+                if (__ballot_sync(FULL, dec)) {
+                    any = true;
+                    if (lane == 0) __stcg(a.stamp + vv, s);
+                    for (int32_t e = cbeg + lane; e < cend; e += 32) nxt[__ldg(&a.adj[e].x)] = 1;
+                }
+                if (!more) break;
+            }
+        }
+        any = __syncthreads_or(any);
+        if (any && threadIdx.x == 0) vctrl[C_SLOT0 + s % 3] = 1;
+        if (!grid_barrier(a.ctrl, s_ok)) {
+            if (threadIdx.x == 0) atomicOr(&a.stat->err, a.ctrl[C_ERR]);
+            return -1;
+        }
+        if (vctrl[C_SLOT0 + s % 3] == 0) return s + 1;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&a.stat->err, (uint32_t)EMV_DEV_SWEEP_LIMIT);
+    return -1;
+}
+
 // Multi-source shortest-path closure of up to 32*VEC rows (R:2109-2130): for
 // every row X of the chunk, d[X][v] = min over u of init[u] + dist(u, v).
 // One cooperative persistent launch:
-//   A. transpose the rows into a vertex-major buffer: vertex v owns one
-//      record of R = 32*VEC int32 (lane l holds rows l*VEC .. l*VEC+VEC-1);
-//      in level-1 mode the rows are the k single-source initialisations;
-//   B. frontier sweeps: a warp takes 8 vertices at once, reads their active
-//      flags and CSR bounds with one load each, and for every
-//      active vertex pulls min over its arcs (u, w) of rec[u] + w -- one
-//      coalesced 128*VEC-byte gather per arc, 2 KB in flight per warp -- and writes
-//      the record in place.  Only the owner writes a record and values only
-//      decrease, so no atomics are needed; a vertex that decreased marks its
-//      neighbours active for the next sweep.  Sweeps end when one changes
-//      nothing (bounded by n + 1, the Bellman-Ford bound);
-//   C. transpose back into the table rows.
-// Buffer reads use ld.global.cg (L2), never a stale L1 line.
+//   A. transpose the rows into vertex-major records (vertex v owns 32*VEC
+//      int32, element e = row e, 128*VEC bytes); in level-1 mode the rows are
+//      the k single-source initialisations;
+//   B. frontier sweeps (relax_sweeps), bounded by n + 1 (the Bellman-Ford
+//      bound), ending after a sweep that changes nothing;
+//   C. transpose the records back into the table rows.
+// Records and stamps are read with ld.global.cg (L2), never through a stale
+// L1 line.
 template <int VEC>
 __global__ void __launch_bounds__(RELAX_THREADS, 2) k_relax(RelaxArgs a)
 {
-    using V = typename IVec<VEC>::T;
-    constexpr int R = 32 * VEC;
-    constexpr int GROUP = VEC == 4 ? 4 : 8;  // gathers in flight per warp: 2 KB for VEC >= 2
-    constexpr int TASK_V = 8;                  // vertices per warp task
     __shared__ int32_t tile[32][33];
     __shared__ int s_ok;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwb = blockDim.x >> 5;
     const int32_t n = a.n;
     const int32_t ntiles = (n + 31) >> 5;
     const int32_t nrows = a.nrows;
-    int32_t *buf = a.scratch;
+    constexpr int R = 32 * VEC;
 
     // ---- A: rows -> vertex-major records
     for (int32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
@@ -294,12 +404,9 @@ __global__ void __launch_bounds__(RELAX_THREADS, 2) k_relax(RelaxArgs a)
                 tile[r][lane] = x;
             }
             __syncthreads();
-            // record of vertex vv: element (l*VEC + j) holds row l*VEC + j
             for (int vv = warp; vv < 32; vv += nwb) {
                 const int32_t v2 = t * 32 + vv;
-                if (v2 < n) {
-                    __stcg(buf + (int64_t)v2 * R + g * 32 + lane, tile[lane][vv]);  // element e holds row e
-                }
+                if (v2 < n) __stcg(a.scratch + (int64_t)v2 * R + g * 32 + lane, tile[lane][vv]);
             }
             __syncthreads();
         }
@@ -307,90 +414,24 @@ __global__ void __launch_bounds__(RELAX_THREADS, 2) k_relax(RelaxArgs a)
     for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
         a.act0[v] = 1;
         a.act1[v] = 0;
+        a.stamp[v] = -1;
     }
     if (!grid_barrier(a.ctrl, &s_ok)) {
         if (threadIdx.x == 0) atomicOr(&a.stat->err, a.ctrl[C_ERR]);
         return;
     }
 
-    // ---- B: frontier sweeps (a warp task is TASK_V consecutive vertices)
-    const int32_t gw = (int32_t)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    const int32_t nwg = (int32_t)((gridDim.x * blockDim.x) >> 5);
-    const int32_t ntasks = (n + TASK_V - 1) / TASK_V;
-    volatile uint32_t *vctrl = a.ctrl;
-    const V *recs = reinterpret_cast<const V *>(buf);
-    int32_t s = 0;
-    bool converged = false;
-    for (; s < a.max_sweeps; s++) {
-        uint8_t *cur = (s & 1) ? a.act1 : a.act0;
-        uint8_t *nxt = (s & 1) ? a.act0 : a.act1;
-        if (blockIdx.x == 0 && threadIdx.x == 0) vctrl[C_SLOT0 + (s + 1) % 3] = 0;
-        bool any = false;
-        for (int32_t blk = gw; blk < ntasks; blk += nwg) {
-            const int32_t v = blk * TASK_V + lane;
-            const bool f = lane < TASK_V && v < n && __ldcg(cur + v) != 0;
-            unsigned act = __ballot_sync(FULL, f);
-            if (!act) continue;
-            if (f) cur[v] = 0;
-            const int32_t rp0 = (lane < TASK_V && v < n) ? __ldg(a.row_ptr + v) : 0;
-            const int32_t rp1 = (lane < TASK_V && v < n) ? __ldg(a.row_ptr + v + 1) : 0;
-            while (act) {
-                const int j = __ffs(act) - 1;
-                act &= act - 1;
-                const int32_t vv = blk * TASK_V + j;
-                const int32_t beg = __shfl_sync(FULL, rp0, j), end = __shfl_sync(FULL, rp1, j);
-                V *mine = reinterpret_cast<V *>(buf + (int64_t)vv * R) + lane;
-                const V old = __ldcg(mine);
-                V acc = old;
-                for (int32_t e0 = beg; e0 < end; e0 += 32) {
-                    int2 arc = make_int2(0, 0);
-                    if (e0 + lane < end) arc = __ldg(a.adj + e0 + lane);
-                    const int cnt = min(32, end - e0);
-                    for (int g = 0; g < cnt; g += GROUP) {
-                        V val[GROUP];
-                        int32_t wt[GROUP];
-#pragma unroll
-                        for (int i = 0; i < GROUP; i++) {
-                            const int32_t u = __shfl_sync(FULL, arc.x, (g + i) & 31);
-                            wt[i] = __shfl_sync(FULL, arc.y, (g + i) & 31);
-                            val[i] = (g + i < cnt) ? __ldcg(recs + (int64_t)u * 32 + lane) : vinf<V>();
-                        }
-#pragma unroll
-                        for (int i = 0; i < GROUP; i++) acc = vmin(acc, vadd(val[i], wt[i]));
-                    }
-                }
-                const bool dec = vlt(acc, old);
-                if (dec) __stcg(mine, acc);
-                if (__ballot_sync(FULL, dec)) {
-                    any = true;
-                    for (int32_t e = beg + lane; e < end; e += 32) nxt[__ldg(&a.adj[e].x)] = 1;
-                }
-            }
-        }
-        any = __syncthreads_or(any);
-        if (any && threadIdx.x == 0) vctrl[C_SLOT0 + s % 3] = 1;
-        if (!grid_barrier(a.ctrl, &s_ok)) {
-            if (threadIdx.x == 0) atomicOr(&a.stat->err, a.ctrl[C_ERR]);
-            return;
-        }
-        if (vctrl[C_SLOT0 + s % 3] == 0) {
-            converged = true;
-            s++;
-            break;
-        }
-    }
-    if (!converged) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&a.stat->err, (uint32_t)EMV_DEV_SWEEP_LIMIT);
-        return;
-    }
+    // ---- B
+    const int32_t s = relax_sweeps<VEC>(a, &s_ok);
+    if (s < 0) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.stat->sweeps, (unsigned long long)s);
 
-    // ---- C: vertex-major records -> rows
+    // ---- C: records -> rows
     for (int32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         for (int g = 0; g < VEC; g++) {
             for (int vv = warp; vv < 32; vv += nwb) {
                 const int32_t v2 = t * 32 + vv;
-                tile[vv][lane] = (v2 < n) ? __ldcg(buf + (int64_t)v2 * R + g * 32 + lane) : INF;
+                tile[vv][lane] = (v2 < n) ? __ldcg(a.scratch + (int64_t)v2 * R + g * 32 + lane) : INF;
             }
             __syncthreads();
             const int32_t v = t * 32 + lane;

@@ -35,6 +35,7 @@ struct emv_ctx {
     int relax_blocks_max[3] = {0, 0, 0};  // cooperative grid of k_relax<1>, <2>, <4>
     DevBuf ctrl, stat;             // relaxation barrier words, solve status
     DevBuf scratch, act;           // vertex-major chunk buffer, active flags
+    DevBuf stamp;                  // per vertex: last sweep in which it changed
     DevBuf adj;                    // packed (col, w) arcs
     DevBuf xs, terms;              // subsets by level, terminals
     DevBuf g_row, g_col, g_w;      // device copy of a host CSR
