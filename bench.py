@@ -277,11 +277,11 @@ def run_single(args, dist: Dist) -> dict:
     relax_launches = 1 + sum(-(-comb(k, mm) // 128) for mm in range(2, k + 1))  # 128-row chunks
     peak = measured_peaks()
     if relax_ms >= merge_ms:
-        kname, kms, launches_k = "k_relax_chunk", relax_ms, relax_launches
+        kname, kms, launches_k = "k_relax", relax_ms, relax_launches
         alg = rows * relax_bytes_per_row(n, m)
         unit_note = "12n+16m+4(n+1) bytes per row closure x 4095 rows"
     else:
-        kname, kms, launches_k = "k_merge", merge_ms, k - 1
+        kname, kms, launches_k = "k_merge_stream", merge_ms, k - 1
         alg = merge_bytes(n, k)
         unit_note = "12 bytes per (X,Y,v) triple x n(3^k-2^(k+1)+1)"
     achieved = alg / (kms / 1000.0) / 1e9
