@@ -37,6 +37,8 @@ sys.path.insert(0, ROOT)
 
 SINGLE = dict(n=100000, degree=20, wmin=1, wmax=100, k=12, seed=123456789)
 SINGLE_NAME = "single large plain solve: random 20-regular n=100000 m=1e6 w=[1,100] k=12 seed=123456789"
+ROOFLINE = dict(n=1 << 20, degree=10, wmin=1, wmax=1024, k=14, seed=123456789)
+ROOFLINE_NAME = "roofline-scale solve: random 10-regular n=2^20 m=5*2^20 w=[1,1024] k=14 seed=123456789 (64 GiB table)"
 PROFILES = os.path.join(ROOT, "profiles")
 
 
@@ -46,7 +48,7 @@ def parse_args():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    p.add_argument("--workload", choices=["single", "batched", "serve"], default="single")
+    p.add_argument("--workload", choices=["single", "roofline", "batched", "serve"], default="single")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--batch-count", type=int, default=4096)
     p.add_argument("--serve-rates", type=str, default="2000,8000")
@@ -208,7 +210,7 @@ def cpu_reference_runs(steps: int, warmup: int, threads: int | None = None) -> d
     return {"kind": kind, "threads": threads, "runs_s": runs}
 
 
-def run_single(args, dist: Dist) -> dict:
+def run_single(args, dist: Dist, cfg: dict = SINGLE, cfg_name: str = SINGLE_NAME) -> dict:
     import numpy as np
     import torch
 
@@ -217,7 +219,7 @@ def run_single(args, dist: Dist) -> dict:
     E.build()
     dev = torch.device("cuda", dist.local)
     torch.cuda.set_device(dev)
-    inst = E.StpInstance.regular(**SINGLE)
+    inst = E.StpInstance.regular(**cfg)
     csr = E.Csr.from_stp(inst)
     n, m, k = csr.n, inst.m, csr.k
     row = torch.from_numpy(csr.row_ptr).to(dev)
@@ -281,11 +283,11 @@ def run_single(args, dist: Dist) -> dict:
         alg = rows * relax_bytes_per_row(n, m)
         unit_note = "12n+16m+4(n+1) bytes per row closure x 4095 rows"
     else:
-        kname, kms, launches_k = "k_merge_stream", merge_ms, k - 1
+        kname, kms, launches_k = ("k_merge_stream" if cfg is SINGLE else "merge"), merge_ms, k - 1
         alg = merge_bytes(n, k)
         unit_note = "12 bytes per (X,Y,v) triple x n(3^k-2^(k+1)+1)"
     achieved = alg / (kms / 1000.0) / 1e9
-    prof = profile_traffic(f"{kname}_single")
+    prof = profile_traffic(f"{kname}_single") if cfg is SINGLE else None
     traffic = None
     if prof and "dram_bytes_per_solve" in prof:
         traffic = prof["dram_bytes_per_solve"] / launches_k
@@ -299,9 +301,9 @@ def run_single(args, dist: Dist) -> dict:
            "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": round(ms / args.steps, 3),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
            "data": "synthetic (seeded generator, configuration-model random regular graph)",
-           "config": {"workload": SINGLE_NAME, "n": n, "m": m, "k": k, "table_bytes": 4 * n << k,
+           "config": {"workload": cfg_name, "n": n, "m": m, "k": k, "table_bytes": 4 * n << k,
                       "parallelism": f"replicas x{dist.world}",
-                      "l2": "no flush: 1.7 GB working set per step > 129 MB L2"},
+                      "l2": f"no flush: {4 * (n << k) / 1e9:.1f} GB table per step > 129 MB L2"},
            "cost": cost,
            "e2e": {"value": round(args.steps * dist.world / e2e_s, 4), "unit": "solves/s",
                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -315,7 +317,7 @@ def run_single(args, dist: Dist) -> dict:
            "roofline": roofline,
            "clocks": clk.summary()}
     solver.close()
-    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline and cfg is SINGLE:
         c = cpu_reference_runs(steps=1, warmup=0)
         t = statistics.median(c["runs_s"])
         out["cpu_baseline"] = {"value": round(1.0 / t, 5), "unit": "solves/s", "cores": c["threads"],
@@ -352,6 +354,8 @@ def main():
             out = run_reference(args, dist)
         elif args.workload == "single":
             out = run_single(args, dist)
+        elif args.workload == "roofline":
+            out = run_single(args, dist, ROOFLINE, ROOFLINE_NAME)
         elif args.workload == "batched":
             from steiner_edge_linear_gb300 import benchmarks
             out = benchmarks.run_batched(args, dist)

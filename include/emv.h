@@ -112,6 +112,21 @@ int emv_gen_regular(int64_t n, int32_t degree, int32_t wmin, int32_t wmax,
 int emv_gen_mixed(uint64_t base_seed, int64_t index, int32_t nmin, int32_t nmax,
                   int32_t kmin, int32_t kmax, int32_t group_pct, emv_stp **out);
 
+/* Power-law random multigraph by the configuration model: `classes` degree
+ * classes whose sizes grow geometrically and whose degrees follow size^alpha
+ * (alpha < 0) with mean `degree`; connected, weights in [wmin, wmax], k
+ * distinct terminals.  Replaces gen-unique's "powlaw" mode
+ * (graph-gen/gen-unique.c:409-470, 534-543). */
+int emv_gen_powlaw(int64_t n, int32_t degree, double alpha, int32_t classes,
+                   int32_t wmin, int32_t wmax, int32_t k, uint64_t seed,
+                   emv_stp **out);
+
+/* Complete graph on n vertices, weights in [wmin, wmax], k distinct
+ * terminals.  Replaces gen-unique's "clique" mode (gen-unique.c:559-571),
+ * which builds a clique on sqrt(n*d/2) of n vertices. */
+int emv_gen_clique(int64_t n, int32_t wmin, int32_t wmax, int32_t k,
+                   uint64_t seed, emv_stp **out);
+
 /* ----------------------------------------------------------- GPU solver */
 
 typedef struct emv_ctx emv_ctx;

@@ -111,6 +111,9 @@ SIGNATURES = {
     "emv_gen_regular": (ctypes.c_int, [_I64, _I32, _I32, _I32, _I32, _U64, ctypes.POINTER(ctypes.POINTER(_Stp))]),
     "emv_gen_mixed": (ctypes.c_int, [_U64, _I64, _I32, _I32, _I32, _I32, _I32,
                                      ctypes.POINTER(ctypes.POINTER(_Stp))]),
+    "emv_gen_powlaw": (ctypes.c_int, [_I64, _I32, ctypes.c_double, _I32, _I32, _I32, _I32, _U64,
+                                      ctypes.POINTER(ctypes.POINTER(_Stp))]),
+    "emv_gen_clique": (ctypes.c_int, [_I64, _I32, _I32, _I32, _U64, ctypes.POINTER(ctypes.POINTER(_Stp))]),
     "emv_create": (ctypes.c_int, [ctypes.POINTER(_P), _I32]),
     "emv_destroy": (ctypes.c_int, [_P]),
     "emv_kernel_dev": (ctypes.c_int, [_P, _I32, _I64, _P, _P, _P, _I32, _P, _P, _I64, ctypes.POINTER(_I64), _P]),
@@ -219,6 +222,21 @@ class StpInstance:
         """Instance ``index`` of the mixed batched distribution (emv_gen_mixed)."""
         p = ctypes.POINTER(_Stp)()
         _check(load_library().emv_gen_mixed(base_seed, index, nmin, nmax, kmin, kmax, group_pct, ctypes.byref(p)))
+        return StpInstance._take(p)
+
+    @staticmethod
+    def powlaw(n: int, degree: int, alpha: float, classes: int, wmin: int, wmax: int, k: int,
+               seed: int) -> "StpInstance":
+        """Power-law random instance (emv_gen_powlaw)."""
+        p = ctypes.POINTER(_Stp)()
+        _check(load_library().emv_gen_powlaw(n, degree, alpha, classes, wmin, wmax, k, seed, ctypes.byref(p)))
+        return StpInstance._take(p)
+
+    @staticmethod
+    def clique(n: int, wmin: int, wmax: int, k: int, seed: int) -> "StpInstance":
+        """Complete-graph instance (emv_gen_clique)."""
+        p = ctypes.POINTER(_Stp)()
+        _check(load_library().emv_gen_clique(n, wmin, wmax, k, seed, ctypes.byref(p)))
         return StpInstance._take(p)
 
     def write(self, path: str) -> None:

@@ -423,13 +423,19 @@ struct Dsu {
     }
 };
 
-// Configuration-model pairing of n*d stubs, redrawn from the same stream until connected.
-int regular_edges(Rng &rng, int64_t n, int32_t d, int32_t wmin, int32_t wmax, std::vector<int64_t> &edges)
+// Configuration-model pairing of the stubs of a degree sequence (vertex v
+// holds deg[v] stubs), redrawn from the same stream until connected.
+int config_edges(Rng &rng, const std::vector<int32_t> &deg, int32_t wmin, int32_t wmax, std::vector<int64_t> &edges)
 {
-    const int64_t stubs = n * d, m = stubs / 2;
-    std::vector<int32_t> st((size_t)stubs);
+    const int64_t n = (int64_t)deg.size();
+    int64_t stubs = 0;
+    for (int32_t d : deg) stubs += d;
+    const int64_t m = stubs / 2;
+    std::vector<int32_t> st((size_t)stubs), owner((size_t)stubs);
+    for (int64_t v = 0, pos = 0; v < n; v++)
+        for (int32_t j = 0; j < deg[(size_t)v]; j++) owner[(size_t)pos++] = (int32_t)v;
     for (int attempt = 0; attempt < 1000; attempt++) {
-        for (int64_t i = 0; i < stubs; i++) st[(size_t)i] = (int32_t)(i / d);
+        for (int64_t i = 0; i < stubs; i++) st[(size_t)i] = owner[(size_t)i];
         for (int64_t i = stubs - 1; i > 0; i--) {
             int64_t j = (int64_t)rng.below((uint64_t)i + 1);
             std::swap(st[(size_t)i], st[(size_t)j]);
@@ -447,6 +453,56 @@ int regular_edges(Rng &rng, int64_t n, int32_t d, int32_t wmin, int32_t wmax, st
         if (comps == 1) return EMV_OK;
     }
     return emv_fail(EMV_ERR_DISCONNECTED, "generator: no connected pairing in 1000 draws");
+}
+
+int regular_edges(Rng &rng, int64_t n, int32_t d, int32_t wmin, int32_t wmax, std::vector<int64_t> &edges)
+{
+    return config_edges(rng, std::vector<int32_t>((size_t)n, d), wmin, wmax, edges);
+}
+
+double det_pow(double x, double y) { return det_exp2(y * det_log2(x)); }  // x > 0
+
+// Power-law degree sequence with `classes` degree classes (gen-unique.c's
+// mkpowlawdist, graph-gen/gen-unique.c:409-470, restated): class sizes grow
+// geometrically, f_j ~ b^j with sum n (b by bisection); degrees follow
+// f_j^alpha scaled so that the mean degree is d; the total is made even.
+int powlaw_degrees(int64_t n, int32_t d, double alpha, int32_t classes, std::vector<int32_t> &deg)
+{
+    double lo = 1.0, hi = det_exp2(det_log2((double)n) / (double)(classes - 1)), b = lo;
+    for (int it = 0; it < 200; it++) {
+        b = 0.5 * (lo + hi);
+        double s = 0, p = 1;
+        for (int32_t j = 0; j < classes; j++) { s += p; p *= b; }
+        if (s < (double)n) lo = b; else hi = b;
+    }
+    std::vector<int64_t> freq((size_t)classes);
+    int64_t fsum = 0;
+    double p = b;
+    for (int32_t j = 0; j < classes; j++) {
+        const double cum = (1.0 - p) / (1.0 - b);
+        freq[(size_t)j] = std::max<int64_t>(1, (int64_t)(cum - (double)fsum + 0.5));
+        fsum += freq[(size_t)j];
+        p *= b;
+    }
+    freq[(size_t)classes - 1] += n - fsum;  // exact total n
+    if (freq[(size_t)classes - 1] < 1) return emv_fail(EMV_ERR_BAD_INPUT, "generator: too many degree classes");
+    double norm = 0;
+    for (int64_t f : freq) norm += det_pow((double)f, alpha + 1.0);
+    const double scale = (double)d * (double)n / norm;
+    std::vector<int32_t> cdeg((size_t)classes);
+    for (int32_t j = 0; j < classes; j++) {
+        const double x = scale * det_pow((double)freq[(size_t)j], alpha);
+        cdeg[(size_t)j] = (int32_t)std::min<double>(std::max<double>(1.0, x + 0.5), (double)(n - 1));
+    }
+    deg.clear();
+    int64_t total = 0;
+    for (int32_t j = 0; j < classes; j++)
+        for (int64_t i = 0; i < freq[(size_t)j]; i++) {
+            deg.push_back(cdeg[(size_t)j]);
+            total += cdeg[(size_t)j];
+        }
+    if (total % 2) deg[0]++;
+    return EMV_OK;
 }
 
 void sample_distinct(Rng &rng, int64_t n, int32_t k, std::vector<int64_t> &out)
@@ -538,4 +594,49 @@ extern "C" int emv_gen_mixed(uint64_t base_seed, int64_t index, int32_t nmin, in
         terms.push_back(n + g);
     }
     return make_stp(n + groups, edges, terms, out);
+}
+
+extern "C" int emv_gen_powlaw(int64_t n, int32_t degree, double alpha, int32_t classes, int32_t wmin, int32_t wmax,
+                              int32_t k, uint64_t seed, emv_stp **out)
+{
+    if (!out) return emv_fail(EMV_ERR_BAD_INPUT, "null argument");
+    *out = nullptr;
+    if (n < 2 || n >= INT32_MAX / 64 || degree < 1 || !(alpha < 0.0) || classes < 2 || classes > n)
+        return emv_fail(EMV_ERR_BAD_INPUT, "generator: need alpha < 0, 2 <= classes <= n");
+    if (wmin < 0 || wmax < wmin || wmax >= EMV_INF32) return emv_fail(EMV_ERR_BAD_INPUT, "generator: weight range");
+    if (k < 1 || k > n) return emv_fail(EMV_ERR_BAD_INPUT, "generator: k out of range");
+    std::vector<int32_t> deg;
+    int st = powlaw_degrees(n, degree, alpha, classes, deg);
+    if (st) return st;
+    Rng rng(seed);
+    // vertex ids are shuffled so that degree does not follow the id
+    std::vector<int64_t> perm;
+    sample_distinct(rng, n, (int32_t)n, perm);
+    std::vector<int32_t> pdeg((size_t)n);
+    for (int64_t i = 0; i < n; i++) pdeg[(size_t)perm[(size_t)i]] = deg[(size_t)i];
+    std::vector<int64_t> edges, terms;
+    st = config_edges(rng, pdeg, wmin, wmax, edges);
+    if (st) return st;
+    sample_distinct(rng, n, k, terms);
+    return make_stp(n, edges, terms, out);
+}
+
+extern "C" int emv_gen_clique(int64_t n, int32_t wmin, int32_t wmax, int32_t k, uint64_t seed, emv_stp **out)
+{
+    if (!out) return emv_fail(EMV_ERR_BAD_INPUT, "null argument");
+    *out = nullptr;
+    if (n < 2 || n > 46341) return emv_fail(EMV_ERR_BAD_INPUT, "generator: clique of n in [2, 46341]");
+    if (wmin < 0 || wmax < wmin || wmax >= EMV_INF32) return emv_fail(EMV_ERR_BAD_INPUT, "generator: weight range");
+    if (k < 1 || k > n) return emv_fail(EMV_ERR_BAD_INPUT, "generator: k out of range");
+    Rng rng(seed);
+    std::vector<int64_t> edges, terms;
+    edges.reserve((size_t)(n * (n - 1) / 2 * 3));
+    for (int64_t u = 0; u < n; u++)
+        for (int64_t v = u + 1; v < n; v++) {
+            edges.push_back(u);
+            edges.push_back(v);
+            edges.push_back(wmin + (int64_t)rng.below((uint64_t)(wmax - wmin) + 1));
+        }
+    sample_distinct(rng, n, k, terms);
+    return make_stp(n, edges, terms, out);
 }

@@ -172,3 +172,55 @@ def test_cli_reference_lines(emv, tmp_path):
     inst.write(path)
     r = subprocess.run([emv.CLI_PATH, "-in", path, "-el"], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
     assert r.returncode != 0 and "min_cost != cost" in r.stderr
+
+
+def test_cli_dijkstra_command(emv, orc, tmp_path):
+    """-dijkstra (R:2454-2484): source = rand() % n after srand(seed), distances on the GPU."""
+    import ctypes
+    import re
+
+    inst = emv.StpInstance.regular(5000, 6, 1, 1000, 3, 4)
+    path = str(tmp_path / "d.stp")
+    inst.write(path)
+    out = subprocess.run([emv.CLI_PATH, "-in", path, "-dijkstra", "-seed", "77"], stdout=subprocess.PIPE, text=True,
+                         check=True).stdout
+    mt = re.search(r"dijkstra: \[source: (\d+)\] \[total: (.*) ms (.*)GiB/s\] \[reached: (\d+)\] \[max: (\d+)\]", out)
+    assert mt, out
+    libc = ctypes.CDLL(None)
+    libc.srand(77)
+    src = libc.rand() % inst.n
+    assert int(mt.group(1)) == src + 1
+    csr = emv.Csr.from_stp(inst)
+    d = orc.sssp(csr.n, csr.row_ptr, csr.col, csr.w, src)
+    assert int(mt.group(4)) == inst.n and int(mt.group(5)) == int(d.max())
+
+
+def test_roofline_scale_solve(emv, orc):
+    """n = 2^20, degree 10, k = 14 (the 64 GiB table): exact rows over the
+    first 6 terminals against the oracle and the closure/monotonicity
+    properties on sampled rows."""
+    torch = pytest.importorskip("torch")
+    inst = emv.StpInstance.regular(1 << 20, 10, 1, 1024, 14, 123456789)
+    csr = emv.Csr.from_stp(inst)
+    assert csr.check() < emv.INF32
+    dev = torch.device("cuda:0")
+    row, col, w = (torch.from_numpy(a).to(dev) for a in (csr.row_ptr, csr.col, csr.w))
+    n, k = csr.n, csr.k
+    table = torch.empty(((1 << k), n), dtype=torch.int32, device=dev)
+    with emv.Solver(0) as s:
+        cost = s.kernel_dev(n, csr.arcs, row.data_ptr(), col.data_ptr(), w.data_ptr(), csr.terminals,
+                            table.data_ptr(), n, torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    want, _ = orc.emv_table(n, csr.row_ptr, csr.col, csr.w, csr.terminals[:6], threads=16)
+    assert np.array_equal(table[:64].cpu().numpy(), want)
+    assert cost == int(table[(1 << (k - 1)) - 1, int(csr.terminals[k - 1])])
+    src = np.repeat(np.arange(n), np.diff(csr.row_ptr))
+    rng = np.random.default_rng(3)
+    for X in rng.integers(1, 1 << k, size=4):
+        r = table[int(X)].cpu().numpy()
+        assert (r[csr.col] <= r[src] + csr.w).all()
+        for b in range(k):
+            if X >> b & 1 and X ^ (1 << b):
+                assert (table[int(X) ^ (1 << b)].cpu().numpy() <= r).all()
+    del table
+    torch.cuda.empty_cache()

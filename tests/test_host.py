@@ -186,3 +186,16 @@ def test_cli_parse_error_exits_nonzero(emv, tmp_path):
         f.write(B01_LIKE.replace("edges 6", "edges 9"))
     r = subprocess.run([emv.CLI_PATH, "-in", path, "-el"], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True)
     assert r.returncode != 0 and "ERROR" in r.stderr
+
+
+def test_generator_powlaw_and_clique(emv):
+    g = emv.StpInstance.powlaw(20000, 6, -0.5, 10, 1, 100, 8, 5)
+    deg = np.bincount(g.edges[:, :2].reshape(-1), minlength=g.n)
+    assert abs(deg.mean() - 6) < 0.2 and deg.max() > 20 * deg.min()  # heavy tail
+    emv.Csr.from_stp(g).check()
+    again = emv.StpInstance.powlaw(20000, 6, -0.5, 10, 1, 100, 8, 5)
+    assert np.array_equal(again.edges, g.edges) and np.array_equal(again.terminals, g.terminals)
+    q = emv.StpInstance.clique(60, 1, 50, 6, 3)
+    assert q.m == 60 * 59 // 2 and len(set(q.terminals.tolist())) == 6
+    with pytest.raises(emv.EmvError):
+        emv.StpInstance.powlaw(100, 4, 0.5, 5, 1, 10, 3, 1)  # alpha must be negative
