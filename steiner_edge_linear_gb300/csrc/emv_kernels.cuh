@@ -182,40 +182,77 @@ struct MergePhase {
     int32_t npairs;         // per subset, multiple of 4
 };
 
-// Streamed subset merge of level m (R:2068-2107) with a lane per vertex at
-// every level.  Block = 32 consecutive vertices; the minima of all C(k,m)
-// subsets live in shared memory (acc) while the phases j = 1..m/2 stage only
-// the rows of sizes j and m-j; lanes read consecutive words of a staged row,
-// so the pair loop is free of bank conflicts.
-// Subsets with few pairs per warp (the top levels) split their list over
-// several warps; partial minima meet in acc through shared-memory atomicMin.
-// The terminal override of the virtual-source arcs (R:2099-2107) is applied
-// last, from the finished level m-1 rows in the table.
+// Streamed subset merge of level m (R:2068-2107).  Block = 32 consecutive
+// vertices; the minima of all C(k,m) subsets live in shared memory (acc)
+// while the phases j = 1..m/2 stage only the rows of sizes j and m-j.
+// The pair loop runs on quarter-warps: the 8 lanes of a quarter hold 4
+// vertices each, so one 16-byte shared load per lane brings a whole staged
+// row (128 bytes, one conflict-free wavefront per quarter) and one decoded
+// pair serves 32 vertices; the four quarters of a warp take four different
+// subsets.  Subsets with few pairs (the top levels) split their list over
+// several quarters; partial minima meet in acc through shared-memory
+// atomicMin.  The terminal override of the virtual-source arcs
+// (R:2099-2107) is applied last, from the finished level m-1 rows.
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)), "l"(gmem)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+__device__ __forceinline__ void merge_pair4(uint4 &a, const uint4 *__restrict__ S4, uint32_t pr)
+{
+    const uint4 y = S4[(pr & 0xffffu) * 8];
+    const uint4 z = S4[(pr >> 16) * 8];
+    a.x = min(a.x, y.x + z.x);
+    a.y = min(a.y, y.y + z.y);
+    a.z = min(a.z, y.z + z.z);
+    a.w = min(a.w, y.w + z.w);
+}
+
 __global__ void __launch_bounds__(1024) k_merge_stream(int32_t *__restrict__ table, int64_t ld, int32_t n,
                                                        const uint32_t *__restrict__ xs_level, int32_t cnt,
                                                        const MergePhase *__restrict__ phases, int32_t nphase,
                                                        const int32_t *__restrict__ terms, int32_t k)
 {
-    extern __shared__ uint32_t sm[];
+    extern __shared__ __align__(16) uint32_t sm[];
     uint32_t *acc = sm;
     uint32_t *S = sm + (size_t)cnt * 32;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int nq = nw * 4, qid = warp * 4 + (lane >> 3), ql = lane & 7;
     const int32_t v0 = blockIdx.x * 32, v = v0 + lane;
     for (int32_t i = threadIdx.x; i < cnt * 32; i += blockDim.x) acc[i] = (uint32_t)INF;
-    const int parts = cnt >= nw ? 1 : nw / cnt;
+    const int parts = cnt >= nq ? 1 : nq / cnt;
+    const uint4 *S4 = reinterpret_cast<const uint4 *>(S) + ql;  // staged row r, this lane's 4 vertices: S4[r * 8]
+    const uint4 inf4 = make_uint4((uint32_t)INF, (uint32_t)INF, (uint32_t)INF, (uint32_t)INF);
     for (int32_t ph = 0; ph < nphase; ph++) {
         const MergePhase P = phases[ph];
         __syncthreads();
-        for (int32_t i = warp; i <= P.nrows; i += nw)
-            S[i * 32 + lane] = (i < P.nrows && v < n) ? (uint32_t)__ldg(table + (int64_t)__ldg(P.rows + i) * ld + v)
-                                                      : (uint32_t)INF;
+        if (v0 + 32 <= n) {
+            // staging of a full vertex block: 4-byte asynchronous copies, so a
+            // warp has all its rows in flight at once (row ids 32 at a time)
+            for (int32_t c0 = warp * 32; c0 < P.nrows; c0 += nw * 32) {
+                const uint32_t myr = c0 + lane < P.nrows ? __ldg(P.rows + c0 + lane) : 0u;
+                const int32_t nr = min(32, P.nrows - c0);
+                for (int32_t j = 0; j < nr; j++) {
+                    const uint32_t r = __shfl_sync(FULL, myr, j);
+                    cp_async4(S + (c0 + j) * 32 + lane, table + (int64_t)r * ld + v);
+                }
+            }
+            if (warp == nw - 1) S[P.nrows * 32 + lane] = (uint32_t)INF;
+            cp_async_wait_all();
+        } else {
+            for (int32_t i = warp; i <= P.nrows; i += nw)
+                S[i * 32 + lane] = (i < P.nrows && v < n)
+                                       ? (uint32_t)__ldg(table + (int64_t)__ldg(P.rows + i) * ld + v)
+                                       : (uint32_t)INF;
+        }
         __syncthreads();
         const int32_t quads = P.npairs >> 2;
-        const uint32_t *Sl = S + lane;
-        for (int32_t t = warp; t < cnt * parts; t += nw) {
+        for (int32_t t = qid; t < cnt * parts; t += nq) {
             const int32_t xi = t / parts, part = t - xi * parts;
             const uint4 *Q = reinterpret_cast<const uint4 *>(P.pairs + (int64_t)xi * P.npairs);
-            uint32_t a0 = (uint32_t)INF, a1 = (uint32_t)INF;
+            uint4 a0 = inf4, a1 = inf4;
             int32_t qi = part;
             // two quads of pairs in flight ahead of the one being reduced
             const uint4 zq = make_uint4(0, 0, 0, 0);
@@ -224,15 +261,26 @@ __global__ void __launch_bounds__(1024) k_merge_stream(int32_t *__restrict__ tab
             while (qi < quads) {
                 const int32_t q2i = qi + 2 * parts;
                 const uint4 q2 = q2i < quads ? __ldg(Q + q2i) : zq;
-                a0 = min(a0, Sl[(q.x & 0xffffu) * 32] + Sl[(q.x >> 16) * 32]);
-                a1 = min(a1, Sl[(q.y & 0xffffu) * 32] + Sl[(q.y >> 16) * 32]);
-                a0 = min(a0, Sl[(q.z & 0xffffu) * 32] + Sl[(q.z >> 16) * 32]);
-                a1 = min(a1, Sl[(q.w & 0xffffu) * 32] + Sl[(q.w >> 16) * 32]);
+                merge_pair4(a0, S4, q.x);
+                merge_pair4(a1, S4, q.y);
+                merge_pair4(a0, S4, q.z);
+                merge_pair4(a1, S4, q.w);
                 q = q1;
                 q1 = q2;
                 qi += parts;
             }
-            atomicMin(acc + xi * 32 + lane, min(a0, a1));
+            uint32_t *A = acc + xi * 32 + ql * 4;
+            const uint4 r = make_uint4(min(a0.x, a1.x), min(a0.y, a1.y), min(a0.z, a1.z), min(a0.w, a1.w));
+            if (parts == 1) {
+                uint4 *A4 = reinterpret_cast<uint4 *>(A);
+                const uint4 o = *A4;
+                *A4 = make_uint4(min(o.x, r.x), min(o.y, r.y), min(o.z, r.z), min(o.w, r.w));
+            } else {
+                atomicMin(A + 0, r.x);
+                atomicMin(A + 1, r.y);
+                atomicMin(A + 2, r.z);
+                atomicMin(A + 3, r.w);
+            }
         }
     }
     __syncthreads();
@@ -368,29 +416,15 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
     return -1;
 }
 
-// Multi-source shortest-path closure of up to 32*VEC rows (R:2109-2130): for
-// every row X of the chunk, d[X][v] = min over u of init[u] + dist(u, v).
-// One cooperative persistent launch:
-//   A. transpose the rows into vertex-major records (vertex v owns 32*VEC
-//      int32, element e = row e, 128*VEC bytes); in level-1 mode the rows are
-//      the k single-source initialisations;
-//   B. frontier sweeps (relax_sweeps), bounded by n + 1 (the Bellman-Ford
-//      bound), ending after a sweep that changes nothing;
-//   C. transpose the records back into the table rows.
-// Records and stamps are read with ld.global.cg (L2), never through a stale
-// L1 line.
+// Phase A of a relaxation chunk: rows -> vertex-major records (vertex v owns
+// 32*VEC int32, element e = row e); in level-1 mode the rows are the k
+// single-source initialisations.  Also resets the active flags and stamps.
 template <int VEC>
-__global__ void __launch_bounds__(RELAX_THREADS, 2) k_relax(RelaxArgs a)
+__device__ void relax_load_records(const RelaxArgs &a, int32_t (*tile)[33])
 {
-    __shared__ int32_t tile[32][33];
-    __shared__ int s_ok;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwb = blockDim.x >> 5;
-    const int32_t n = a.n;
-    const int32_t ntiles = (n + 31) >> 5;
-    const int32_t nrows = a.nrows;
+    const int32_t n = a.n, ntiles = (n + 31) >> 5, nrows = a.nrows;
     constexpr int R = 32 * VEC;
-
-    // ---- A: rows -> vertex-major records
     for (int32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int32_t v = t * 32 + lane;
         for (int g = 0; g < VEC; g++) {
@@ -416,17 +450,15 @@ __global__ void __launch_bounds__(RELAX_THREADS, 2) k_relax(RelaxArgs a)
         a.act1[v] = 0;
         a.stamp[v] = -1;
     }
-    if (!grid_barrier(a.ctrl, &s_ok)) {
-        if (threadIdx.x == 0) atomicOr(&a.stat->err, a.ctrl[C_ERR]);
-        return;
-    }
+}
 
-    // ---- B
-    const int32_t s = relax_sweeps<VEC>(a, &s_ok);
-    if (s < 0) return;
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.stat->sweeps, (unsigned long long)s);
-
-    // ---- C: records -> rows
+// Phase C: vertex-major records -> table rows.
+template <int VEC>
+__device__ void relax_store_records(const RelaxArgs &a, int32_t (*tile)[33])
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwb = blockDim.x >> 5;
+    const int32_t n = a.n, ntiles = (n + 31) >> 5, nrows = a.nrows;
+    constexpr int R = 32 * VEC;
     for (int32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         for (int g = 0; g < VEC; g++) {
             for (int vv = warp; vv < 32; vv += nwb) {
@@ -443,6 +475,29 @@ __global__ void __launch_bounds__(RELAX_THREADS, 2) k_relax(RelaxArgs a)
             __syncthreads();
         }
     }
+}
+
+// Multi-source shortest-path closure of up to 32*VEC rows (R:2109-2130): for
+// every row X of the chunk, d[X][v] = min over u of init[u] + dist(u, v).
+// One cooperative persistent launch: A. rows -> vertex-major records;
+// B. frontier sweeps (relax_sweeps), bounded by n + 1 (the Bellman-Ford
+// bound), ending after a sweep that changes nothing; C. records -> rows.
+// Records and stamps are read with ld.global.cg (L2), never through a stale
+// L1 line.
+template <int VEC>
+__global__ void __launch_bounds__(RELAX_THREADS, 2) k_relax(RelaxArgs a)
+{
+    __shared__ int32_t tile[32][33];
+    __shared__ int s_ok;
+    relax_load_records<VEC>(a, tile);
+    if (!grid_barrier(a.ctrl, &s_ok)) {
+        if (threadIdx.x == 0) atomicOr(&a.stat->err, a.ctrl[C_ERR]);
+        return;
+    }
+    const int32_t s = relax_sweeps<VEC>(a, &s_ok);
+    if (s < 0) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.stat->sweeps, (unsigned long long)s);
+    relax_store_records<VEC>(a, tile);
 }
 
 // ------------------------------------------------------------- traceback
