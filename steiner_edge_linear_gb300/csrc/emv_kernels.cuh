@@ -302,8 +302,10 @@ __global__ void __launch_bounds__(1024) k_merge_stream(int32_t *__restrict__ tab
     }
 }
 
-// Frontier sweeps over one chunk (phase B of k_relax).  A warp takes TASK_V
-// vertices, reads their active flags and CSR bounds with one load each, and
+// Frontier sweeps over one chunk (phase B of k_relax).  A warp owns a
+// contiguous range of n / W vertices (W warps in the grid, so the shares
+// differ by one vertex at most) and takes them TASK_V at a time: it
+// reads their active flags and CSR bounds with one load each, and
 // for every active vertex pulls min over its arcs (u, w) of rec[u] + w with
 // coalesced 128*VEC-byte gathers -- only from heads stamped as changed in the
 // previous sweep (a head that last changed earlier was already pulled when
@@ -321,7 +323,8 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
     const int32_t n = a.n;
     const int32_t gw = (int32_t)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int32_t nwg = (int32_t)((gridDim.x * blockDim.x) >> 5);
-    const int32_t ntasks = (n + TASK_V - 1) / TASK_V;
+    // each warp owns a contiguous range of n / (warps) vertices, scanned TASK_V at a time
+    const int32_t vbeg = (int32_t)((int64_t)n * gw / nwg), vend = (int32_t)((int64_t)n * (gw + 1) / nwg);
     volatile uint32_t *vctrl = a.ctrl;
     const V *recs = reinterpret_cast<const V *>(a.scratch);  // vertex v: recs[v * 32 .. v * 32 + 31]
     int32_t s = 0;
@@ -330,14 +333,15 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
         uint8_t *nxt = (s & 1) ? a.act0 : a.act1;
         if (blockIdx.x == 0 && threadIdx.x == 0) vctrl[C_SLOT0 + (s + 1) % 3] = 0;
         bool any = false;
-        for (int32_t blk = gw; blk < ntasks; blk += nwg) {
-            const int32_t v = blk * TASK_V + lane;
-            const bool f = lane < TASK_V && v < n && __ldcg(cur + v) != 0;
+        for (int32_t base = vbeg; base < vend; base += TASK_V) {
+            const int32_t v = base + lane;
+            const bool mine = lane < TASK_V && v < vend;
+            const bool f = mine && __ldcg(cur + v) != 0;
             unsigned act = __ballot_sync(FULL, f);
             if (!act) continue;
             if (f) cur[v] = 0;
-            const int32_t rp0 = (lane < TASK_V && v < n) ? __ldg(a.row_ptr + v) : 0;
-            const int32_t rp1 = (lane < TASK_V && v < n) ? __ldg(a.row_ptr + v + 1) : 0;
+            const int32_t rp0 = mine ? __ldg(a.row_ptr + v) : 0;
+            const int32_t rp1 = mine ? __ldg(a.row_ptr + v + 1) : 0;
             // first active vertex: bounds, first 32 arcs and their selection
             int j = __ffs(act) - 1;
             act &= act - 1;
@@ -349,7 +353,7 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
                 pull = s == 0 || __ldcg(a.stamp + arc.x) >= s - 1;
             }
             for (;;) {
-                const int32_t vv = blk * TASK_V + j;
+                const int32_t vv = base + j;
                 V *mine = reinterpret_cast<V *>(a.scratch + (int64_t)vv * 32 * VEC) + lane;
                 const V old = __ldcg(mine);
                 V acc = old;
