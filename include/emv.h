@@ -127,6 +127,37 @@ int emv_gen_powlaw(int64_t n, int32_t degree, double alpha, int32_t classes,
 int emv_gen_clique(int64_t n, int32_t wmin, int32_t wmax, int32_t k,
                    uint64_t seed, emv_stp **out);
 
+/* ------------------------------------------------ binary instance container */
+
+/* A packed container of one or more instances in the solver's input form: the
+ * int32 CSR of emv_csr_build plus the terminals, and optionally the STP edge
+ * list, so that ingress (the CLI's -bin, batches, the server) reads arrays
+ * instead of parsing text.  The reference's experiment driver passes "-bin"
+ * (experiments/report.py:265-266, 457-470) but neither its generator nor its
+ * reader implements a binary format, so this format has no reference
+ * counterpart.  Layout (little-endian, arrays padded to 8 bytes):
+ *   "EMVBIN01", u64 count, u64 offset[count]; at each offset:
+ *   i64 n, m, k, cost (-1: none), flags (bit 0: edge list present),
+ *   i32 row_ptr[n+1], col[2m], w[2m], terminals[k], [edges[3m]: u, v, w]. */
+typedef struct emv_bin emv_bin;
+
+/* Writes `count` instances (CSR built as emv_csr_build does); with_edges
+ * keeps each STP edge list so emv_bin_stp can restore it exactly. */
+int emv_bin_write(const char *path, const emv_stp *const *insts, int32_t count,
+                  int32_t with_edges);
+/* Reads a whole container; EMV_ERR_PARSE when it is not one. */
+int emv_bin_open(const char *path, emv_bin **out);
+int32_t emv_bin_count(const emv_bin *b);
+/* Views of instance `index` inside the container (valid until emv_bin_close),
+ * ready for emv_solve / emv_batch_solve / emv_server_submit.  The first access
+ * checks the record (sizes, prefix sums, heads, weights, terminals, edge list
+ * against degrees): a corrupt record is EMV_ERR_PARSE, never a bad read. */
+int emv_bin_instance(emv_bin *b, int32_t index, struct emv_instance *inst,
+                     int64_t *cost);
+/* STP form of an instance written with its edge list (free with emv_stp_free). */
+int emv_bin_stp(emv_bin *b, int32_t index, emv_stp **out);
+void emv_bin_close(emv_bin *b);
+
 /* ----------------------------------------------------------- GPU solver */
 
 typedef struct emv_ctx emv_ctx;

@@ -132,6 +132,12 @@ SIGNATURES = {
     "emv_server_cancel": (ctypes.c_int, [_P, _I64]),
     "emv_server_stats_get": (ctypes.c_int, [_P, ctypes.POINTER(_ServerStats)]),
     "emv_server_destroy": (ctypes.c_int, [_P]),
+    "emv_bin_write": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.POINTER(_Stp)), _I32, _I32]),
+    "emv_bin_open": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_P)]),
+    "emv_bin_count": (_I32, [_P]),
+    "emv_bin_instance": (ctypes.c_int, [_P, _I32, ctypes.POINTER(_Instance), ctypes.POINTER(_I64)]),
+    "emv_bin_stp": (ctypes.c_int, [_P, _I32, ctypes.POINTER(ctypes.POINTER(_Stp))]),
+    "emv_bin_close": (None, [_P]),
 }
 
 _lib: Optional[ctypes.CDLL] = None
@@ -285,6 +291,71 @@ class Csr:
         g = self.c_graph()
         _check(load_library().emv_graph_check(ctypes.byref(g), ctypes.byref(b)))
         return int(b.value)
+
+
+class BinContainer:
+    """EMVBIN01 container of instances in solver form (emv_bin_*): int32 CSR,
+    terminals, cost and optionally the STP edge list.  The reference's
+    experiment driver passes "-bin" (experiments/report.py:265-266) but has no
+    binary reader; this format is the solver's own."""
+
+    def __init__(self, path: str):
+        self._lib = load_library()
+        self._b = ctypes.c_void_p()
+        _check(self._lib.emv_bin_open(path.encode(), ctypes.byref(self._b)))
+
+    @staticmethod
+    def write(path: str, instances: Sequence["StpInstance"], with_edges: bool = True) -> None:
+        keep = []
+        arr = (ctypes.POINTER(_Stp) * len(instances))()
+        for i, g in enumerate(instances):
+            e = np.ascontiguousarray(g.edges, dtype=np.int64).reshape(-1)
+            t = np.ascontiguousarray(g.terminals, dtype=np.int64)
+            st = _Stp(g.n, g.m, g.k, g.cost, e.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                      t.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)))
+            keep.append((e, t, st))
+            arr[i] = ctypes.pointer(st)
+        _check(load_library().emv_bin_write(path.encode(), arr, len(instances), int(bool(with_edges))))
+
+    def __len__(self) -> int:
+        return int(self._lib.emv_bin_count(self._b))
+
+    def csr(self, index: int) -> "Csr":
+        """Instance `index` as a Csr (arrays copied out of the container)."""
+        inst = _Instance()
+        cost = ctypes.c_int64()
+        _check(self._lib.emv_bin_instance(self._b, index, ctypes.byref(inst), ctypes.byref(cost)))
+        n, arcs, k = int(inst.g.n), int(inst.g.arcs), int(inst.k)
+
+        def view(ptr, count):
+            return np.ctypeslib.as_array(ctypes.cast(ptr, ctypes.POINTER(ctypes.c_int32)), shape=(count,)).copy()
+
+        empty = np.zeros(0, np.int32)
+        return Csr(n, view(inst.g.row_ptr, n + 1), view(inst.g.col, arcs) if arcs else empty,
+                   view(inst.g.w, arcs) if arcs else empty, view(inst.terminals, k), int(cost.value))
+
+    def stp(self, index: int) -> "StpInstance":
+        """Instance `index` in STP form (needs the edge list in the container)."""
+        p = ctypes.POINTER(_Stp)()
+        _check(self._lib.emv_bin_stp(self._b, index, ctypes.byref(p)))
+        return StpInstance._take(p)
+
+    def close(self) -> None:
+        if self._b:
+            self._lib.emv_bin_close(self._b)
+            self._b = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 @dataclass

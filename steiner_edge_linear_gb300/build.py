@@ -35,6 +35,7 @@ SOURCES = [
     "emv_batch.cu",
     "emv_server.cpp",
     "emv_noalloc.cu",
+    "emv_bin.cpp",
 ]
 CLI_SOURCES = ["cli.cpp"]
 

@@ -2,6 +2,9 @@
 //
 // Same flags as reader-el's main() (reader/reader-el.c:2368-2412):
 //   -in <file> (else stdin), -el / -erickson, -list, -seed <n>, -dijkstra, -h / -help
+// plus -bin (the input is an EMVBIN01 container, see emv_bin_open; the
+// reference's report.py passes -bin but its reader has no binary format) and
+// -index <i> (which instance of the container, default 0)
 // and the same stdout lines (R:2414-2437, R:603-614, R:735-896, R:2445,
 // R:2298-2340, R:1891-1903, R:2500-2528), so the reference's scripts parse
 // them unchanged.  As in the reference, a "cost" line in the input that
@@ -50,7 +53,8 @@ int main(int argc, char **argv)
 {
     const double t_main = now_ms();
     long seed = 123456789;
-    bool have_seed = false, list_soln = false, file_input = false;
+    bool have_seed = false, list_soln = false, file_input = false, bin_input = false;
+    long bin_index = 0;
     int cmd = 0;  // 0 nop, 1 dijkstra, 2 edge-linear
     const char *filename = nullptr;
     for (int f = 1; f < argc; f++) {
@@ -58,6 +62,11 @@ int main(int argc, char **argv)
         if (!std::strcmp(argv[f], "-dijkstra")) cmd = 1;
         if (!std::strcmp(argv[f], "-el") || !std::strcmp(argv[f], "-erickson")) cmd = 2;
         if (!std::strcmp(argv[f], "-list")) list_soln = true;
+        if (!std::strcmp(argv[f], "-bin")) bin_input = true;
+        if (!std::strcmp(argv[f], "-index")) {
+            if (f == argc - 1) die("main", "%s", "instance index missing from command line");
+            bin_index = std::atol(argv[++f]);
+        }
         if (!std::strcmp(argv[f], "-in")) {
             if (f == argc - 1) die("main", "%s", "file name missing from command line");
             filename = argv[++f];
@@ -72,7 +81,8 @@ int main(int argc, char **argv)
             std::printf("usage: %s -in <input graph> <arguments>\n\narguments :\n"
                         "\t-seed : seed value\n\t-el : Erickson-Monma-Veinott algorithm\n"
                         "\t-dijkstra : Dijkstra single source shortest path\n"
-                        "\t-list : Output Steiner tree\n\n",
+                        "\t-list : Output Steiner tree\n"
+                        "\t-bin : input is an EMVBIN01 container (-index <i> selects the instance)\n\n",
                         argv[0]);
             return 0;
         }
@@ -85,39 +95,63 @@ int main(int argc, char **argv)
     std::printf("random seed = %ld\n", seed);
     std::fflush(stdout);
 
-    // graph_load (R:473-618)
+    // graph_load (R:473-618), or a container record read as arrays
     double t0 = now_ms();
     emv_stp *g = nullptr;
-    int st = emv_stp_load(file_input ? filename : nullptr, &g);
-    if (st) die_status("graph_load", st);
+    emv_bin *bin = nullptr;
+    emv_instance binst{};
+    int64_t n = 0, m = 0, k = 0, stp_cost = -1;
+    int st;
+    if (bin_input) {
+        if (!file_input) die("main", "%s", "-bin needs -in <file>");
+        st = emv_bin_open(filename, &bin);
+        if (!st) st = emv_bin_instance(bin, (int32_t)bin_index, &binst, &stp_cost);
+        if (st) die_status("graph_load", st);
+        n = binst.g.n;
+        m = binst.g.arcs / 2;
+        k = binst.k;
+    } else {
+        st = emv_stp_load(file_input ? filename : nullptr, &g);
+        if (st) die_status("graph_load", st);
+        n = g->n;
+        m = g->m;
+        k = g->k;
+        stp_cost = g->cost;
+    }
     std::printf("input: n = %lld, m = %lld, k = %lld, cost = %lld [%.2lf ms] {peak: %.2lfGiB} {curr: %.2lfGiB}\n",
-                (long long)g->n, (long long)g->m, (long long)g->k, (long long)g->cost, now_ms() - t0, 0.0, 0.0);
+                (long long)n, (long long)m, (long long)k, (long long)stp_cost, now_ms() - t0, 0.0, 0.0);
     std::printf("terminals:");
-    for (int64_t i = 0; i < g->k; i++) std::printf(" %lld", (long long)g->terminals[i] + 1);
+    for (int64_t i = 0; i < k; i++)
+        std::printf(" %lld", (long long)(bin ? binst.terminals[i] : g->terminals[i]) + 1);
     std::printf("\n");
     std::fflush(stdout);
 
-    // root_build (R:706-899): CSR and the terminal index.
+    // root_build (R:706-899): CSR and the terminal index (a container holds the CSR already).
     const double t_rb = now_ms();
     std::printf("root build: ");
     double t1 = now_ms();
-    std::vector<int32_t> row((size_t)g->n + 1), col((size_t)(2 * g->m)), w((size_t)(2 * g->m));
+    std::vector<int32_t> row, col, w;
+    if (!bin) {
+        row.resize((size_t)n + 1);
+        col.resize((size_t)(2 * m));
+        w.resize((size_t)(2 * m));
+    }
     std::printf("[zero: %.2lf ms] ", now_ms() - t1);
     t1 = now_ms();
-    st = emv_csr_build(g->n, g->m, g->edges, row.data(), col.data(), w.data());
-    if (st) die_status("root_build", st);
+    if (!bin) {
+        st = emv_csr_build(n, m, g->edges, row.data(), col.data(), w.data());
+        if (st) die_status("root_build", st);
+    }
     const double t_csr = now_ms() - t1;
     std::printf("[pos: %.2lf ms] [adj: %.2lf ms] ", t_csr * 0.5, t_csr * 0.5);
     t1 = now_ms();
-    std::vector<int32_t> kk((size_t)g->k);
-    for (int64_t i = 0; i < g->k; i++) kk[(size_t)i] = (int32_t)g->terminals[i];
+    std::vector<int32_t> kk((size_t)k);
+    for (int64_t i = 0; i < k; i++) kk[(size_t)i] = bin ? binst.terminals[i] : (int32_t)g->terminals[i];
     std::printf("[term: %.2lf ms] ", now_ms() - t1);
-    const int64_t host_bytes = (int64_t)(row.size() + col.size() + w.size()) * 4;
+    const int64_t host_bytes = (4 * (n + 1) + 16 * m);
     std::printf("done. [%.2lf ms] {peak: %.2lfGiB} {curr: %.2lfGiB}\n", now_ms() - t_rb, gib(host_bytes),
                 gib(host_bytes));
-    const int64_t stp_cost = g->cost;
-    const int64_t n = g->n, m = g->m, k = g->k;
-    emv_graph graph{(int32_t)n, 2 * m, row.data(), col.data(), w.data()};
+    emv_graph graph = bin ? binst.g : emv_graph{(int32_t)n, 2 * m, row.data(), col.data(), w.data()};
 
     static const char *legend[] = {"no operation", "Dijkstra Single-Source-Shortest-Path", "Erickson-Monma-Veinott"};
     std::printf("command: %s\n", legend[cmd]);
@@ -193,6 +227,7 @@ int main(int argc, char **argv)
     }
     if (ctx) emv_destroy(ctx);
     emv_stp_free(g);
+    emv_bin_close(bin);
     std::printf("command done [%.2lf ms]\n", now_ms() - t_cmd);
     std::printf("grand total [%.2lf ms] {peak: %.2lfGiB}\n", now_ms() - t_main, gib(dev_peak + host_bytes));
     struct utsname un;
