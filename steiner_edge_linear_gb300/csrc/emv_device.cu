@@ -177,95 +177,179 @@ constexpr int32_t MERGE_SMEM_KMAX = 15;  // staged slots must fit 16 bits
 
 constexpr int32_t STREAM_SMEM_BYTES = 224 * 1024;
 
-// Plan of the streamed merge (k_merge_stream) for every level of k: phases
-// j = 1..m/2 staging the rows of sizes j and m-j, with each subset's pairs as
-// staged positions.  A level whose accumulators plus largest phase exceed the
-// shared memory keeps the staged-all-lower-rows kernel.
+// Plan of the streamed merge (k_merge_stream) for every level of k.  The
+// subsets of level m are cut into groups whose accumulators (128 bytes per
+// subset and 32 vertices) leave room for staged rows; for each group and each
+// j = 1..m/2 the pairs {Y, X\Y} with |Y| = j are cut into phases whose rows
+// fit the rest of the shared memory, taking the Y's in level order, each with
+// all the X\Y it pairs with in the group.  Several group sizes are planned
+// and the one staging the fewest rows is kept; up to k = 12 that is the whole
+// level in one group with one phase per j.  A level with no workable plan
+// keeps the staged-all-lower-rows kernel.
+namespace {
+
+struct HostPhase {
+    size_t rows_at, qoff_at, pairs_at;
+    int32_t nrows;
+};
+struct HostGroup {
+    int64_t x0, cnt, smem;
+    std::vector<HostPhase> phases;
+};
+
+// Plans level m with groups of at most gx subsets into `data` (offsets
+// relative to its start); returns false when a group cannot hold one pair.
+bool plan_level(const std::vector<uint32_t> &xs, const std::vector<int64_t> &off, const std::vector<uint32_t> &rank,
+                std::vector<int32_t> &pos, int32_t m, int64_t gx, int64_t smem_bytes, std::vector<uint32_t> &data,
+                std::vector<HostGroup> &groups, int64_t &cost)
+{
+    const int64_t lvl = off[(size_t)m], cnt = off[(size_t)m + 1] - lvl;
+    const int64_t cap = smem_bytes / 128 - gx - 1;  // staged rows besides the INF pad row
+    if (cap < 2) return false;
+    data.clear();
+    groups.clear();
+    cost = 0;
+    struct Entry {
+        uint32_t ry, xi, y, z;
+    };
+    std::vector<Entry> ent;
+    std::vector<std::vector<uint32_t>> per_x;
+    std::vector<uint32_t> rows;
+    for (int64_t x0 = 0; x0 < cnt; x0 += gx) {
+        const int64_t g = std::min(gx, cnt - x0);
+        HostGroup G{x0, g, 0, {}};
+        per_x.assign((size_t)g, {});
+        int64_t max_rows = 0;
+        auto emit = [&]() {
+            if (rows.empty()) return;
+            HostPhase hp;
+            hp.nrows = (int32_t)rows.size();
+            hp.rows_at = data.size();
+            data.insert(data.end(), rows.begin(), rows.end());
+            hp.qoff_at = data.size();
+            uint32_t q = 0;
+            for (int64_t x = 0; x < g; x++) {
+                data.push_back(q);
+                q += (uint32_t)((per_x[(size_t)x].size() + 3) / 4);
+            }
+            data.push_back(q);
+            while (data.size() % 4) data.push_back(0);  // pairs are read as uint4: 16-byte aligned
+            hp.pairs_at = data.size();
+            const uint32_t pad = (uint32_t)hp.nrows | ((uint32_t)hp.nrows << 16);
+            for (int64_t x = 0; x < g; x++) {
+                std::vector<uint32_t> &l = per_x[(size_t)x];
+                while (l.size() % 4) l.push_back(pad);
+                data.insert(data.end(), l.begin(), l.end());
+                cost += (int64_t)l.size() / 4;  // padded pair quads
+                l.clear();
+            }
+            for (uint32_t r : rows) pos[r] = -1;
+            max_rows = std::max<int64_t>(max_rows, hp.nrows);
+            cost += hp.nrows + 32;
+            rows.clear();
+            G.phases.push_back(hp);
+        };
+        for (int32_t j = 1; 2 * j <= m; j++) {
+            const bool same = (j == m - j);
+            ent.clear();
+            for (int64_t x = 0; x < g; x++) {
+                const uint32_t X = xs[(size_t)(lvl + x0 + x)];
+                const uint32_t low = X & (0u - X);
+                for (uint32_t Y = (X - 1) & X; Y; Y = (Y - 1) & X) {
+                    if (__builtin_popcount(Y) != j || (same && !(Y & low))) continue;
+                    ent.push_back({rank[Y], (uint32_t)x, Y, X ^ Y});
+                }
+            }
+            std::stable_sort(ent.begin(), ent.end(), [](const Entry &a, const Entry &b) { return a.ry < b.ry; });
+            for (const Entry &e : ent) {
+                const int64_t need = (pos[e.y] < 0) + (pos[e.z] < 0 && e.z != e.y);
+                if ((int64_t)rows.size() + need > cap) emit();
+                if (pos[e.y] < 0) {
+                    pos[e.y] = (int32_t)rows.size();
+                    rows.push_back(e.y);
+                }
+                if (pos[e.z] < 0) {
+                    pos[e.z] = (int32_t)rows.size();
+                    rows.push_back(e.z);
+                }
+                per_x[e.xi].push_back((uint32_t)pos[e.y] | ((uint32_t)pos[e.z] << 16));
+            }
+            emit();
+        }
+        G.smem = (g + max_rows + 1) * 128;
+        cost += 64;
+        groups.push_back(std::move(G));
+    }
+    return true;
+}
+
+}  // namespace
+
 int plan_stream_merge(emv_ctx *c, int32_t k, cudaStream_t st)
 {
     const std::vector<uint32_t> &xs = c->xs_host;
     const std::vector<int64_t> &off = c->xs_off;
-    c->mstream_phase_off.assign((size_t)k + 2, 0);
-    c->mstream_nphase.assign((size_t)k + 2, 0);
-    c->mstream_smem.assign((size_t)k + 2, 0);
+    c->mstream_groups.assign((size_t)k + 2, {});
     if (k > MERGE_SMEM_KMAX) return EMV_OK;
     std::vector<uint32_t> rank((size_t)1 << k, 0);  // position within its level
     for (int32_t m = 1; m <= k; m++)
         for (int64_t i = off[(size_t)m]; i < off[(size_t)m + 1]; i++) rank[xs[(size_t)i]] = (uint32_t)(i - off[(size_t)m]);
-    struct HostPhase {
-        size_t rows_at, pairs_at;
-        int32_t nrows, npairs;
-    };
-    std::vector<uint32_t> data;
-    std::vector<std::vector<HostPhase>> plan((size_t)k + 2);
+    std::vector<int32_t> pos((size_t)1 << k, -1);
+    std::vector<uint32_t> data, tmp, best_data;
+    std::vector<HostGroup> tmp_groups, best_groups;
+    std::vector<std::vector<HostGroup>> plan((size_t)k + 2);
     for (int32_t m = 2; m <= k; m++) {
         const int64_t cnt = off[(size_t)m + 1] - off[(size_t)m];
-        const int64_t acc_bytes = cnt * 128;
-        int64_t worst = 0;
-        for (int32_t j = 1; 2 * j <= m; j++) {
-            const int64_t ny = off[(size_t)j + 1] - off[(size_t)j], nz = off[(size_t)(m - j) + 1] - off[(size_t)(m - j)];
-            const int64_t nrows = (j == m - j) ? ny : ny + nz;
-            worst = std::max(worst, (nrows + 1) * 128);
-        }
-        if (acc_bytes + worst > STREAM_SMEM_BYTES) continue;  // not streamed
-        for (int32_t j = 1; 2 * j <= m; j++) {
-            const bool same = (j == m - j);
-            const int64_t yb = off[(size_t)j], ny = off[(size_t)j + 1] - yb;
-            const int64_t zb = off[(size_t)(m - j)], nz = off[(size_t)(m - j) + 1] - zb;
-            HostPhase hp;
-            hp.rows_at = data.size();
-            for (int64_t i = 0; i < ny; i++) data.push_back(xs[(size_t)(yb + i)]);
-            if (!same)
-                for (int64_t i = 0; i < nz; i++) data.push_back(xs[(size_t)(zb + i)]);
-            hp.nrows = (int32_t)(same ? ny : ny + nz);
-            const uint32_t zoff = same ? 0 : (uint32_t)ny, pad = (uint32_t)hp.nrows;
-            // pairs of this phase per subset: all j-subsets Y of X (Y holding X's
-            // lowest terminal when both halves have the same size)
-            int32_t npairs = 0;
-            {
-                int64_t c_mj = 1;
-                for (int32_t i = 0; i < j; i++) c_mj = c_mj * (m - i) / (i + 1);
-                npairs = (int32_t)(same ? c_mj / 2 : c_mj);
+        int64_t best_cost = -1;
+        for (int64_t gx : {cnt, (int64_t)1024, (int64_t)768, (int64_t)512, (int64_t)384, (int64_t)256, (int64_t)128}) {
+            if (gx != cnt && gx >= cnt) continue;
+            int64_t cost;
+            if (!plan_level(xs, off, rank, pos, m, gx, STREAM_SMEM_BYTES, tmp, tmp_groups, cost)) continue;
+            if (best_cost < 0 || cost < best_cost) {
+                best_cost = cost;
+                best_data.swap(tmp);
+                best_groups.swap(tmp_groups);
             }
-            hp.npairs = (npairs + 3) & ~3;
-            while (data.size() % 4) data.push_back(0);  // pairs are read as uint4: 16-byte aligned blocks
-            hp.pairs_at = data.size();
-            for (int64_t xi = 0; xi < cnt; xi++) {
-                const uint32_t X = xs[(size_t)(off[(size_t)m] + xi)];
-                const uint32_t low = X & (0u - X);
-                int32_t got = 0;
-                for (uint32_t Y = (X - 1) & X; Y; Y = (Y - 1) & X) {
-                    if (__builtin_popcount(Y) != j) continue;
-                    if (same && !(Y & low)) continue;
-                    data.push_back(rank[Y] | ((zoff + rank[X ^ Y]) << 16));
-                    got++;
-                }
-                if (got != npairs) return emv_fail(EMV_ERR_INTERNAL, "merge plan: %d pairs, expected %d", got, npairs);
-                for (; got < hp.npairs; got++) data.push_back(pad | (pad << 16));
-            }
-            plan[(size_t)m].push_back(hp);
         }
-        c->mstream_smem[(size_t)m] = acc_bytes + worst;
+        if (best_cost < 0) continue;  // not streamed
+        while (data.size() % 4) data.push_back(0);
+        const size_t rel = data.size();
+        data.insert(data.end(), best_data.begin(), best_data.end());
+        for (HostGroup &G : best_groups)
+            for (HostPhase &hp : G.phases) {
+                hp.rows_at += rel;
+                hp.qoff_at += rel;
+                hp.pairs_at += rel;
+            }
+        plan[(size_t)m] = best_groups;
     }
     if (data.empty()) return EMV_OK;
     int r = dev_reserve(c->mstream_data, sizeof(uint32_t) * data.size());
     if (r) return r;
     std::vector<MergePhase> phases;
     const uint32_t *base = (const uint32_t *)c->mstream_data.ptr;
-    for (int32_t m = 2; m <= k; m++) {
-        c->mstream_phase_off[(size_t)m] = (int64_t)phases.size();
-        c->mstream_nphase[(size_t)m] = (int64_t)plan[(size_t)m].size();
-        for (const HostPhase &hp : plan[(size_t)m]) {
-            if (hp.pairs_at % 4 != 0 || hp.npairs % 4 != 0)
-                return emv_fail(EMV_ERR_INTERNAL, "merge plan: pair block not 16-byte aligned");
-            MergePhase mp;
-            mp.rows = base + hp.rows_at;
-            mp.pairs = base + hp.pairs_at;
-            mp.nrows = hp.nrows;
-            mp.npairs = hp.npairs;
-            phases.push_back(mp);
+    for (int32_t m = 2; m <= k; m++)
+        for (const HostGroup &G : plan[(size_t)m]) {
+            StreamGroup sg;
+            sg.x0 = G.x0;
+            sg.cnt = G.cnt;
+            sg.smem = G.smem;
+            sg.phase_off = (int64_t)phases.size();
+            sg.nphase = (int64_t)G.phases.size();
+            if (sg.smem > STREAM_SMEM_BYTES) return emv_fail(EMV_ERR_INTERNAL, "merge plan: %lld bytes of shared memory",
+                                                             (long long)sg.smem);
+            for (const HostPhase &hp : G.phases) {
+                if (hp.pairs_at % 4 != 0) return emv_fail(EMV_ERR_INTERNAL, "merge plan: pair block not 16-byte aligned");
+                MergePhase mp;
+                mp.rows = base + hp.rows_at;
+                mp.qoff = base + hp.qoff_at;
+                mp.pairs = base + hp.pairs_at;
+                mp.nrows = hp.nrows;
+                mp.pad_ = 0;
+                phases.push_back(mp);
+            }
+            c->mstream_groups[(size_t)m].push_back(sg);
         }
-    }
     r = dev_reserve(c->mstream_phases, sizeof(MergePhase) * std::max<size_t>(1, phases.size()));
     if (r) return r;
     CUDA_TRY(cudaMemcpyAsync(c->mstream_data.ptr, data.data(), sizeof(uint32_t) * data.size(), cudaMemcpyHostToDevice,
@@ -358,13 +442,16 @@ int launch_merge(emv_ctx *c, int32_t *table, int64_t ld, int32_t n, int32_t k, i
     const int64_t nstage = c->xs_off[(size_t)m];
     cudaError_t e = cudaSuccess;
     c->launches++;
-    if (k <= MERGE_SMEM_KMAX && c->mstream_smem[(size_t)m] > 0) {
-        const int64_t b = c->xs_off[(size_t)m], cnt = c->xs_off[(size_t)m + 1] - b;
-        k_merge_stream<<<(unsigned)((n + 31) / 32), 1024, (size_t)c->mstream_smem[(size_t)m], st>>>(
-            table, ld, n, (const uint32_t *)c->xs.ptr + b, (int32_t)cnt,
-            (const MergePhase *)c->mstream_phases.ptr + c->mstream_phase_off[(size_t)m],
-            (int32_t)c->mstream_nphase[(size_t)m], d_terms, k);
-        e = cudaGetLastError();
+    if (k <= MERGE_SMEM_KMAX && !c->mstream_groups[(size_t)m].empty()) {
+        const int64_t b = c->xs_off[(size_t)m];
+        c->launches += (int64_t)c->mstream_groups[(size_t)m].size() - 1;
+        for (const StreamGroup &g : c->mstream_groups[(size_t)m]) {
+            k_merge_stream<<<(unsigned)((n + 31) / 32), 1024, (size_t)g.smem, st>>>(
+                table, ld, n, (const uint32_t *)c->xs.ptr + b + g.x0, (int32_t)g.cnt,
+                (const MergePhase *)c->mstream_phases.ptr + g.phase_off, (int32_t)g.nphase, d_terms, k);
+            e = cudaGetLastError();
+            if (e != cudaSuccess) break;
+        }
     } else if (k <= MERGE_SMEM_KMAX) {
         const int64_t row_bytes = nstage * 4;
         if (row_bytes * 32 <= MERGE_SMEM_BYTES) e = merge_smem_launch<32>(c, table, ld, n, k, m, d_terms, st);

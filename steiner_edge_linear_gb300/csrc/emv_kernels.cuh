@@ -171,20 +171,23 @@ __global__ void __launch_bounds__(1024) k_merge_smem(int32_t *__restrict__ table
     }
 }
 
-// One phase of the streamed merge: the rows of sizes j and m-j staged
-// together, and for every subset X of level m the pairs {Y, X\Y} with
-// |Y| = j as staged positions (posY | posZ << 16), padded with (pad, pad)
-// to a multiple of 4 (pad = nrows, a staged row of INF).
+// One phase of the streamed merge: a set of staged rows (of sizes j and m-j)
+// and, for every subset X of the launch's group, the pairs {Y, X\Y} whose
+// halves are both staged, as staged positions (posY | posZ << 16) padded with
+// (pad, pad) to whole quads (pad = nrows, a staged row of INF).  X's quads are
+// pairs[4 * qoff[x] .. 4 * qoff[x + 1]).
 struct MergePhase {
-    const uint32_t *rows;   // staged subsets, level order
-    const uint32_t *pairs;  // [cnt][npairs]
+    const uint32_t *rows;   // staged subsets
+    const uint32_t *pairs;  // 16-byte aligned
+    const uint32_t *qoff;   // cnt + 1 quad offsets
     int32_t nrows;
-    int32_t npairs;         // per subset, multiple of 4
+    int32_t pad_;
 };
 
 // Streamed subset merge of level m (R:2068-2107).  Block = 32 consecutive
-// vertices; the minima of all C(k,m) subsets live in shared memory (acc)
-// while the phases j = 1..m/2 stage only the rows of sizes j and m-j.
+// vertices; the minima of a group of the level's subsets (all C(k,m) when
+// they fit) live in shared memory (acc) while the phases stage only rows of
+// sizes j and m-j (all of them, or tiles of them for large k).
 // The pair loop runs on quarter-warps: the 8 lanes of a quarter hold 4
 // vertices each, so one 16-byte shared load per lane brings a whole staged
 // row (128 bytes, one conflict-free wavefront per quarter) and one decoded
@@ -248,10 +251,11 @@ __global__ void __launch_bounds__(1024) k_merge_stream(int32_t *__restrict__ tab
                                        : (uint32_t)INF;
         }
         __syncthreads();
-        const int32_t quads = P.npairs >> 2;
         for (int32_t t = qid; t < cnt * parts; t += nq) {
             const int32_t xi = t / parts, part = t - xi * parts;
-            const uint4 *Q = reinterpret_cast<const uint4 *>(P.pairs + (int64_t)xi * P.npairs);
+            const uint32_t qb = __ldg(P.qoff + xi);
+            const int32_t quads = (int32_t)(__ldg(P.qoff + xi + 1) - qb);
+            const uint4 *Q = reinterpret_cast<const uint4 *>(P.pairs) + qb;
             uint4 a0 = inf4, a1 = inf4;
             int32_t qi = part;
             // two quads of pairs in flight ahead of the one being reduced

@@ -29,6 +29,12 @@ void dev_release(DevBuf &b);
 constexpr int MAX_EVENTS = 64;
 constexpr int BATCH_CLASSES = 12;  // (n bucket 0..3) x (k bucket 0..2)
 
+// One launch of the streamed merge: subsets [x0, x0 + cnt) of a level, its
+// phases and its dynamic shared memory.
+struct StreamGroup {
+    int64_t x0, cnt, phase_off, nphase, smem;
+};
+
 struct emv_ctx {
     int device = 0;
     int sms = 0;
@@ -49,9 +55,9 @@ struct emv_ctx {
     DevBuf mpairs, movr;           // merge pair slots and override slots, all levels of xs_k
     std::vector<int64_t> mpair_base, movr_base;  // per level
     bool merge_attr = false;
-    // streamed merge plan of xs_k: per level, its phases (device) and smem bytes (0 = not streamed)
+    // streamed merge plan of xs_k: per level, its subset groups (none = not streamed)
     DevBuf mstream_data, mstream_phases;
-    std::vector<int64_t> mstream_phase_off, mstream_nphase, mstream_smem;
+    std::vector<std::vector<StreamGroup>> mstream_groups;
     int64_t launches = 0;
     // batched launch
     DevBuf bxs, bxs_off;           // subset lists of every k <= BATCH_KMAX

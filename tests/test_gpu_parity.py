@@ -120,6 +120,20 @@ def test_large_single_solve_properties(emv, orc, solver):
     check_tree(csr.n, inst.edges, res.tree, csr.terminals, res.cost)
 
 
+@pytest.mark.parametrize("n,degree,k", [(700, 6, 13), (300, 4, 14), (120, 4, 15)])
+def test_large_k_whole_table(emv, orc, solver, n, degree, k):
+    """k = 13..15 run the streamed merge in subset groups with row tiles; the
+    whole table must still equal the oracle's."""
+    inst = emv.StpInstance.regular(n, degree, 1, 1000, k, 4242 + k)
+    csr = emv.Csr.from_stp(inst)
+    res = solver.solve(csr, tree=True, table=True)
+    want, want_cost = orc.emv_table(csr.n, csr.row_ptr, csr.col, csr.w, csr.terminals, threads=8)
+    assert res.cost == want_cost
+    mism = np.argwhere(res.table != want)
+    assert mism.size == 0, f"{len(mism)} cells differ, first (X, v) = {mism[:5].tolist()}"
+    check_tree(csr.n, inst.edges, res.tree, csr.terminals, res.cost)
+
+
 def test_bad_inputs_report_status(emv, solver):
     disc = emv.StpInstance.from_text(
         "section graph\nnodes 4\nedges 2\ne 1 2 3\ne 3 4 5\nend\nsection terminals\nterminals 2\nt 1\nt 3\nend\n")
