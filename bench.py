@@ -276,12 +276,15 @@ def run_single(args, dist: Dist, cfg: dict = SINGLE, cfg_name: str = SINGLE_NAME
     launches = int(statistics.median(t["launches"] for t in timings))
     rows = (1 << k) - 1
     from math import comb
-    relax_launches = 1 + sum(-(-comb(k, mm) // 128) for mm in range(2, k + 1))  # 128-row chunks
+    # chunk rule of the library (relax_chunk_rows): 128 rows while 512-byte records fit 3/4 of L2, else 256
+    l2 = getattr(torch.cuda.get_device_properties(0), "L2_cache_size", 126 << 20)
+    chunk = 128 if n * 512 <= l2 * 3 // 4 else 256
+    relax_launches = 1 + sum(-(-comb(k, mm) // chunk) for mm in range(2, k + 1))
     peak = measured_peaks()
     if relax_ms >= merge_ms:
         kname, kms, launches_k = "k_relax", relax_ms, relax_launches
         alg = rows * relax_bytes_per_row(n, m)
-        unit_note = "12n+16m+4(n+1) bytes per row closure x 4095 rows"
+        unit_note = f"12n+16m+4(n+1) bytes per row closure x {rows} rows"
     else:
         kname, kms, launches_k = ("k_merge_stream" if cfg is SINGLE else "merge"), merge_ms, k - 1
         alg = merge_bytes(n, k)

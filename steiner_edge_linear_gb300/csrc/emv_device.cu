@@ -84,8 +84,10 @@ extern "C" int emv_create(emv_ctx **out, int32_t device)
     if (!c) return emv_fail(EMV_ERR_OOM, "ctx");
     c->device = device;
     c->sms = prop.multiProcessorCount;
-    const void *relax_fns[3] = {(const void *)k_relax<1>, (const void *)k_relax<2>, (const void *)k_relax<4>};
-    for (int i = 0; i < 3; i++) {
+    c->l2_bytes = prop.l2CacheSize;
+    const void *relax_fns[4] = {(const void *)k_relax<1>, (const void *)k_relax<2>, (const void *)k_relax<4>,
+                                (const void *)k_relax<8>};
+    for (int i = 0; i < 4; i++) {
         int per_sm = 0;
         CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, relax_fns[i], RELAX_THREADS, 0));
         c->relax_blocks_max[i] = std::max(1, per_sm) * c->sms;
@@ -151,8 +153,11 @@ int launch_relax(emv_ctx *c, const int32_t *row_ptr, const int2 *adj, int32_t n,
     a.ctrl = (uint32_t *)c->ctrl.ptr;
     a.stat = (DevStat *)c->stat.ptr;
     a.max_sweeps = n + 1;
-    const int vi = nrows <= 32 ? 0 : nrows <= 64 ? 1 : 2;
-    const void *fn = vi == 0 ? (const void *)k_relax<1> : vi == 1 ? (const void *)k_relax<2> : (const void *)k_relax<4>;
+    const int vi = nrows <= 32 ? 0 : nrows <= 64 ? 1 : nrows <= 128 ? 2 : 3;
+    const void *fn = vi == 0   ? (const void *)k_relax<1>
+                     : vi == 1 ? (const void *)k_relax<2>
+                     : vi == 2 ? (const void *)k_relax<4>
+                               : (const void *)k_relax<8>;
     // A warp per 8 vertices is enough; small graphs use fewer blocks (cheaper barriers).
     const int vpb = 8 * (RELAX_THREADS / 32);
     const int blocks = std::min(c->relax_blocks_max[vi], std::max(1, (n + vpb - 1) / vpb));
@@ -161,6 +166,15 @@ int launch_relax(emv_ctx *c, const int32_t *row_ptr, const int2 *adj, int32_t n,
     CUDA_TRY(cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(RELAX_THREADS), args, 0, st));
     c->launches += 2;
     return EMV_OK;
+}
+
+// Rows per relaxation chunk: 128 while the chunk's 512-byte vertex records
+// fit in three quarters of L2 (the sweeps' gathers are then L2 hits and
+// larger records only add bytes per sweep), else 256, which halves the sweeps
+// of the graphs whose records stream from HBM anyway.
+int32_t relax_chunk_rows(const emv_ctx *c, int32_t n)
+{
+    return (int64_t)n * 512 <= c->l2_bytes * 3 / 4 ? 128 : CHUNK_ROWS;
 }
 
 int reserve_relax(emv_ctx *c, int32_t n)
@@ -502,8 +516,9 @@ int run_dp(emv_ctx *c, int32_t n, const int32_t *row_ptr, const int2 *adj, int32
         r = launch_merge(c, table, ld, n, k, m, d_terms, st);
         if (r) return r;
         CUDA_TRY(cudaEventRecord(E[ev++], st));  // merge end of level m
-        for (int64_t off = 0; off < cnt; off += CHUNK_ROWS) {
-            const int32_t rows = (int32_t)std::min<int64_t>(CHUNK_ROWS, cnt - off);
+        const int32_t chunk = relax_chunk_rows(c, n);
+        for (int64_t off = 0; off < cnt; off += chunk) {
+            const int32_t rows = (int32_t)std::min<int64_t>(chunk, cnt - off);
             r = launch_relax(c, row_ptr, adj, n, ld, table, xs + b + off, rows, d_terms, 0, st);
             if (r) return r;
         }

@@ -54,6 +54,12 @@ template <> struct IVec<2> {
 template <> struct IVec<4> {
     using T = int4;
 };
+struct int8v {  // 8 int32: a lane's share of a 256-row record
+    int4 a, b;
+};
+template <> struct IVec<8> {
+    using T = int8v;
+};
 
 __device__ __forceinline__ int32_t vmin(int32_t a, int32_t b) { return min(a, b); }
 __device__ __forceinline__ int2 vmin(int2 a, int2 b) { return make_int2(min(a.x, b.x), min(a.y, b.y)); }
@@ -67,9 +73,27 @@ __device__ __forceinline__ int4 vadd(int4 a, int32_t w) { return make_int4(a.x +
 __device__ __forceinline__ bool vlt(int32_t a, int32_t b) { return a < b; }
 __device__ __forceinline__ bool vlt(int2 a, int2 b) { return a.x < b.x || a.y < b.y; }
 __device__ __forceinline__ bool vlt(int4 a, int4 b) { return a.x < b.x || a.y < b.y || a.z < b.z || a.w < b.w; }
+__device__ __forceinline__ int8v vmin(int8v x, int8v y) { return {vmin(x.a, y.a), vmin(x.b, y.b)}; }
+__device__ __forceinline__ int8v vadd(int8v x, int32_t w) { return {vadd(x.a, w), vadd(x.b, w)}; }
+__device__ __forceinline__ bool vlt(int8v x, int8v y) { return vlt(x.a, y.a) || vlt(x.b, y.b); }
+// L2-only loads and stores of a lane's share (L1 may hold stale lines of records other SMs write)
+template <typename T> __device__ __forceinline__ T ldcg_v(const T *p) { return __ldcg(p); }
+template <> __device__ __forceinline__ int8v ldcg_v<int8v>(const int8v *p)
+{
+    const int4 *q = reinterpret_cast<const int4 *>(p);
+    return {__ldcg(q), __ldcg(q + 1)};
+}
+template <typename T> __device__ __forceinline__ void stcg_v(T *p, T v) { __stcg(p, v); }
+template <> __device__ __forceinline__ void stcg_v<int8v>(int8v *p, int8v v)
+{
+    int4 *q = reinterpret_cast<int4 *>(p);
+    __stcg(q, v.a);
+    __stcg(q + 1, v.b);
+}
 template <typename T> __device__ __forceinline__ T vinf();
 template <> __device__ __forceinline__ int32_t vinf<int32_t>() { return INF; }
 template <> __device__ __forceinline__ int2 vinf<int2>() { return make_int2(INF, INF); }
 template <> __device__ __forceinline__ int4 vinf<int4>() { return make_int4(INF, INF, INF, INF); }
+template <> __device__ __forceinline__ int8v vinf<int8v>() { return {vinf<int4>(), vinf<int4>()}; }
 
 }  // namespace emv

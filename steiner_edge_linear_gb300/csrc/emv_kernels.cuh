@@ -321,7 +321,7 @@ template <int VEC>
 __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
 {
     using V = typename IVec<VEC>::T;
-    constexpr int GROUP = VEC == 4 ? 4 : 8;  // gathers in flight per group (2 KB for VEC >= 2)
+    constexpr int GROUP = VEC == 8 ? 2 : VEC == 4 ? 4 : 8;  // gathers in flight per group (2 KB for VEC >= 2)
     constexpr int TASK_V = 8;
     const int lane = threadIdx.x & 31;
     const int32_t n = a.n;
@@ -359,7 +359,7 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
             for (;;) {
                 const int32_t vv = base + j;
                 V *mine = reinterpret_cast<V *>(a.scratch + (int64_t)vv * 32 * VEC) + lane;
-                const V old = __ldcg(mine);
+                const V old = ldcg_v(mine);
                 V acc = old;
                 for (int32_t e0 = beg;;) {
                     unsigned sel = __ballot_sync(FULL, pull);
@@ -374,7 +374,7 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
                             sel &= sel - 1;
                             const int32_t u = __shfl_sync(FULL, arc.x, src);
                             wt[g] = __shfl_sync(FULL, arc.y, src);
-                            val[g] = ok[g] ? __ldcg(recs + (int64_t)u * 32 + lane) : vinf<V>();
+                            val[g] = ok[g] ? ldcg_v(recs + (int64_t)u * 32 + lane) : vinf<V>();
                         }
 #pragma unroll
                         for (int g = 0; g < GROUP; g++) acc = vmin(acc, vadd(val[g], wt[g]));
@@ -403,7 +403,7 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
                     }
                 }
                 const bool dec = vlt(acc, old);
-                if (dec) __stcg(mine, acc);
+                if (dec) stcg_v(mine, acc);
                 if (__ballot_sync(FULL, dec)) {
                     any = true;
                     if (lane == 0) __stcg(a.stamp + vv, s);

@@ -38,7 +38,8 @@ struct StreamGroup {
 struct emv_ctx {
     int device = 0;
     int sms = 0;
-    int relax_blocks_max[3] = {0, 0, 0};  // cooperative grid of k_relax<1>, <2>, <4>
+    int relax_blocks_max[4] = {0, 0, 0, 0};  // cooperative grid of k_relax<1>, <2>, <4>, <8>
+    int64_t l2_bytes = 0;
     DevBuf ctrl, stat;             // relaxation barrier words, solve status
     DevBuf scratch, act;           // vertex-major chunk buffer, active flags
     DevBuf stamp;                  // per vertex: last sweep in which it changed
@@ -74,3 +75,4 @@ struct emv_ctx {
 void subset_levels(int32_t k, std::vector<uint32_t> &xs, std::vector<int64_t> &off);
 int prepare_subsets(emv_ctx *c, int32_t k, cudaStream_t st);
 int reserve_relax(emv_ctx *c, int32_t n);
+int32_t relax_chunk_rows(const emv_ctx *c, int32_t n);
