@@ -16,7 +16,7 @@ constexpr uint32_t SPIN_LIMIT = 1u << 22;  // grid-barrier spin iterations (~1 s
 constexpr int TB_STACK = 64;
 
 // ctrl words of one cooperative relaxation launch (zeroed before the launch)
-enum : int { C_BAR_COUNT = 0, C_BAR_GEN = 1, C_ERR = 2, C_SLOT0 = 4, C_WORDS = 8 };
+enum : int { C_BAR_COUNT = 0, C_BAR_GEN = 1, C_ERR = 2, C_SLOT0 = 4, C_CNT0 = 8, C_WORDS = 12 };
 
 // Persistent device status of one solve (zeroed at solve start).
 struct DevStat {

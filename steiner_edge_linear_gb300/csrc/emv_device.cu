@@ -8,6 +8,7 @@
 #include "emv_solver.h"
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <numeric>
@@ -153,6 +154,11 @@ int launch_relax(emv_ctx *c, const int32_t *row_ptr, const int2 *adj, int32_t n,
     a.ctrl = (uint32_t *)c->ctrl.ptr;
     a.stat = (DevStat *)c->stat.ptr;
     a.max_sweeps = n + 1;
+    // Dense sweeps pay off while almost every vertex has a changed neighbour:
+    // with mean degree d and a fraction f of vertices changed, a vertex has none
+    // with probability (1 - f)^d; take every vertex while that is below 10 %.
+    const double deg = (double)c->relax_arcs / (double)n;
+    a.dense_min = deg > 0 ? (int32_t)std::min<double>((double)n, (double)n * (1.0 - std::pow(0.1, 1.0 / deg))) : n;
     const int vi = nrows <= 32 ? 0 : nrows <= 64 ? 1 : nrows <= 128 ? 2 : 3;
     const void *fn = vi == 0   ? (const void *)k_relax<1>
                      : vi == 1 ? (const void *)k_relax<2>
@@ -584,6 +590,7 @@ extern "C" int emv_kernel_dev(emv_ctx *c, int32_t n, int64_t arcs, const int32_t
     c->launches = 0;
     r = dev_reserve(c->adj, sizeof(int2) * (size_t)std::max<int64_t>(arcs, 1));
     if (r) return r;
+    c->relax_arcs = arcs;
     k_pack_adj<<<grid_for(arcs, 256, 4096), 256, 0, st>>>(d_col, d_w, (int2 *)c->adj.ptr, arcs);
     c->launches++;
     return run_dp(c, n, d_row_ptr, (const int2 *)c->adj.ptr, k, terminals, d_table, ld, st, cost_out, nullptr);
@@ -669,6 +676,7 @@ int solve_on_device(emv_ctx *c, int32_t n, int64_t arcs, const int32_t *row_ptr,
 {
     int r = dev_reserve(c->adj, sizeof(int2) * (size_t)std::max<int64_t>(arcs, 1));
     if (r) return r;
+    c->relax_arcs = arcs;
     k_pack_adj<<<grid_for(arcs, 256, 4096), 256, 0, st>>>(col, w, (int2 *)c->adj.ptr, arcs);
     c->launches++;
     const int64_t ld = ((int64_t)n + 31) / 32 * 32;
@@ -765,6 +773,7 @@ extern "C" int emv_sssp(emv_ctx *c, const emv_graph *g, int32_t source, int64_t 
     CUDA_TRY(cudaMemcpyAsync(c->terms.ptr, &source, sizeof(int32_t), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemsetAsync(c->stat.ptr, 0, sizeof(DevStat), st));
     CUDA_TRY(cudaEventRecord(c->ev[0], st));
+    c->relax_arcs = arcs;
     k_pack_adj<<<grid_for(arcs, 256, 4096), 256, 0, st>>>((const int32_t *)c->g_col.ptr, (const int32_t *)c->g_w.ptr,
                                                           (int2 *)c->adj.ptr, arcs);
     r = launch_relax(c, (const int32_t *)c->g_row.ptr, (const int2 *)c->adj.ptr, n, n, (int32_t *)c->table.ptr,

@@ -39,6 +39,7 @@ struct RelaxArgs {
     DevStat *stat;
     int32_t max_sweeps;
     int32_t *stamp;         // n: last sweep in which the vertex changed (-1 none)
+    int32_t dense_min;      // a sweep after one with more changed vertices takes every vertex
 };
 
 __global__ void k_fill(int32_t *__restrict__ p, int64_t count, int32_t value)
@@ -331,16 +332,28 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
     const int32_t vbeg = (int32_t)((int64_t)n * gw / nwg), vend = (int32_t)((int64_t)n * (gw + 1) / nwg);
     volatile uint32_t *vctrl = a.ctrl;
     const V *recs = reinterpret_cast<const V *>(a.scratch);  // vertex v: recs[v * 32 .. v * 32 + 31]
+    __shared__ unsigned s_chg;
+    if (threadIdx.x == 0) s_chg = 0;
+    __syncthreads();
+    // Dense sweeps take every vertex (a vertex with no changed neighbour then
+    // selects no arc) and so need no neighbour flags from the sweep before:
+    // sweep s + 1 is dense when sweep s - 1 changed more than dense_min vertices.
+    bool dense = true;  // sweep 0: every vertex is active
     int32_t s = 0;
     for (; s < a.max_sweeps; s++) {
         uint8_t *cur = (s & 1) ? a.act1 : a.act0;
         uint8_t *nxt = (s & 1) ? a.act0 : a.act1;
-        if (blockIdx.x == 0 && threadIdx.x == 0) vctrl[C_SLOT0 + (s + 1) % 3] = 0;
+        const uint32_t prev_chg = s == 0 ? (uint32_t)n : vctrl[C_CNT0 + (s + 2) % 3];
+        const bool dense_next = prev_chg > (uint32_t)a.dense_min;
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            vctrl[C_SLOT0 + (s + 1) % 3] = 0;
+            vctrl[C_CNT0 + (s + 1) % 3] = 0;
+        }
         bool any = false;
         for (int32_t base = vbeg; base < vend; base += TASK_V) {
             const int32_t v = base + lane;
             const bool mine = lane < TASK_V && v < vend;
-            const bool f = mine && __ldcg(cur + v) != 0;
+            const bool f = mine && (dense || __ldcg(cur + v) != 0);
             unsigned act = __ballot_sync(FULL, f);
             if (!act) continue;
             if (f) cur[v] = 0;
@@ -406,19 +419,28 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
                 if (dec) stcg_v(mine, acc);
                 if (__ballot_sync(FULL, dec)) {
                     any = true;
-                    if (lane == 0) __stcg(a.stamp + vv, s);
-                    for (int32_t e = cbeg + lane; e < cend; e += 32) nxt[__ldg(&a.adj[e].x)] = 1;
+                    if (lane == 0) {
+                        __stcg(a.stamp + vv, s);
+                        atomicAdd(&s_chg, 1u);
+                    }
+                    if (!dense_next)
+                        for (int32_t e = cbeg + lane; e < cend; e += 32) nxt[__ldg(&a.adj[e].x)] = 1;
                 }
                 if (!more) break;
             }
         }
         any = __syncthreads_or(any);
-        if (any && threadIdx.x == 0) vctrl[C_SLOT0 + s % 3] = 1;
+        if (threadIdx.x == 0) {
+            if (any) vctrl[C_SLOT0 + s % 3] = 1;
+            if (s_chg) atomicAdd(a.ctrl + C_CNT0 + s % 3, s_chg);
+            s_chg = 0;
+        }
         if (!grid_barrier(a.ctrl, s_ok)) {
             if (threadIdx.x == 0) atomicOr(&a.stat->err, a.ctrl[C_ERR]);
             return -1;
         }
         if (vctrl[C_SLOT0 + s % 3] == 0) return s + 1;
+        dense = dense_next;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&a.stat->err, (uint32_t)EMV_DEV_SWEEP_LIMIT);
     return -1;
