@@ -345,6 +345,8 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
         uint8_t *nxt = (s & 1) ? a.act0 : a.act1;
         const uint32_t prev_chg = s == 0 ? (uint32_t)n : vctrl[C_CNT0 + (s + 2) % 3];
         const bool dense_next = prev_chg > (uint32_t)a.dense_min;
+        // after a sweep that changed (almost) every vertex, pull every arc without reading stamps
+        const bool pull_all = prev_chg >= (uint32_t)n - (uint32_t)n / 32;
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             vctrl[C_SLOT0 + (s + 1) % 3] = 0;
             vctrl[C_CNT0 + (s + 1) % 3] = 0;
@@ -367,7 +369,7 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
             bool pull = false;
             if (beg + lane < end) {
                 arc = __ldg(a.adj + beg + lane);
-                pull = s == 0 || __ldcg(a.stamp + arc.x) >= s - 1;
+                pull = pull_all || __ldcg(a.stamp + arc.x) >= s - 1;
             }
             for (;;) {
                 const int32_t vv = base + j;
@@ -397,7 +399,7 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
                     pull = false;  // high-degree vertex: next 32 arcs
                     if (e0 + lane < end) {
                         arc = __ldg(a.adj + e0 + lane);
-                        pull = s == 0 || __ldcg(a.stamp + arc.x) >= s - 1;
+                        pull = pull_all || __ldcg(a.stamp + arc.x) >= s - 1;
                     }
                 }
                 // prefetch the next active vertex before finishing this one
@@ -412,7 +414,7 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
                     arc = make_int2(0, 0);
                     if (beg + lane < end) {
                         arc = __ldg(a.adj + beg + lane);
-                        pull = s == 0 || __ldcg(a.stamp + arc.x) >= s - 1;
+                        pull = pull_all || __ldcg(a.stamp + arc.x) >= s - 1;
                     }
                 }
                 const bool dec = vlt(acc, old);
