@@ -314,10 +314,13 @@ __global__ void __launch_bounds__(1024) k_merge_stream(int32_t *__restrict__ tab
 // for every active vertex pulls min over its arcs (u, w) of rec[u] + w with
 // coalesced 128*VEC-byte gathers -- only from heads stamped as changed in the
 // previous sweep (a head that last changed earlier was already pulled when
-// that change marked this vertex active).  The arcs and stamps of the next
-// active vertex are loaded while the current one's gathers are in flight.
-// Only the owner writes a record and values only decrease, so no atomics are
-// needed.  Returns the number of sweeps, or -1 after an error (recorded).
+// that change marked this vertex active).  The selected arcs of a window are
+// compacted into the warp's shared-memory slots, so the gather loop reads one
+// (head, weight) pair per arc instead of searching the selection mask.  The
+// arcs and stamps of the next active vertex are loaded while the current
+// one's gathers are in flight.  Only the owner writes a record and values
+// only decrease, so no atomics are needed.  Returns the number of sweeps, or
+// -1 after an error (recorded).
 template <int VEC>
 __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
 {
@@ -332,6 +335,9 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
     const int32_t vbeg = (int32_t)((int64_t)n * gw / nwg), vend = (int32_t)((int64_t)n * (gw + 1) / nwg);
     volatile uint32_t *vctrl = a.ctrl;
     const V *recs = reinterpret_cast<const V *>(a.scratch);  // vertex v: recs[v * 32 .. v * 32 + 31]
+    __shared__ int2 s_arcs[RELAX_THREADS / 32][32];
+    int2 *warcs = s_arcs[threadIdx.x >> 5];
+    const unsigned lt = (1u << lane) - 1;
     __shared__ unsigned s_chg;
     if (threadIdx.x == 0) s_chg = 0;
     __syncthreads();
@@ -377,23 +383,25 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
                 const V old = ldcg_v(mine);
                 V acc = old;
                 for (int32_t e0 = beg;;) {
-                    unsigned sel = __ballot_sync(FULL, pull);
-                    while (sel) {
+                    const unsigned sel = __ballot_sync(FULL, pull);
+                    const int cnt = __popc(sel);
+                    // selected arcs compacted in this warp's slots
+                    if (pull) warcs[__popc(sel & lt)] = arc;
+                    __syncwarp();
+                    for (int i = 0; i < cnt; i += GROUP) {
                         V val[GROUP];
                         int32_t wt[GROUP];
-                        bool ok[GROUP];
 #pragma unroll
                         for (int g = 0; g < GROUP; g++) {
-                            ok[g] = sel != 0;
-                            const int src = ok[g] ? __ffs(sel) - 1 : 0;
-                            sel &= sel - 1;
-                            const int32_t u = __shfl_sync(FULL, arc.x, src);
-                            wt[g] = __shfl_sync(FULL, arc.y, src);
-                            val[g] = ok[g] ? ldcg_v(recs + (int64_t)u * 32 + lane) : vinf<V>();
+                            const bool ok = i + g < cnt;
+                            const int2 aw = warcs[(i + g) & 31];  // slots past cnt hold stale arcs: not used
+                            wt[g] = ok ? aw.y : 0;
+                            val[g] = ok ? ldcg_v(recs + (int64_t)aw.x * 32 + lane) : vinf<V>();
                         }
 #pragma unroll
                         for (int g = 0; g < GROUP; g++) acc = vmin(acc, vadd(val[g], wt[g]));
                     }
+                    __syncwarp();
                     e0 += 32;
                     if (e0 >= end) break;
                     pull = false;  // high-degree vertex: next 32 arcs
