@@ -5,8 +5,8 @@
 // of independent instances of uneven n and k share one persistent launch.
 // Per level m of an instance (reader/reader-el.c:2033-2131):
 //   merge  -- vertex blocks of 32: every row of size < m is staged in shared
-//             memory as S[Y][32], a warp computes one subset X at a time with
-//             a lane per vertex (R:2068-2107);
+//             memory as S[Y][32], a quarter-warp computes one subset X at a
+//             time with 4 vertices per lane (R:2068-2107);
 //   relax  -- chunks of R rows are loaded into shared memory vertex-major
 //             (stride R+1, conflict-free), and in-place sweeps pull
 //             min(d[u] + w) over the CSR until a sweep changes nothing
@@ -24,14 +24,19 @@ __device__ __forceinline__ int32_t xs_start(const BatchArgs &a, int32_t k, int32
     return __ldg(a.xs_off + k * (BATCH_KMAX + 2) + m);
 }
 
-// Merge of level m for one instance; S holds 2^k * 32 int32.
+// Merge of level m for one instance; S holds 2^k * 32 int32.  The pair
+// loop runs on quarter-warps: the 8 lanes of a quarter hold 4 vertices each
+// (one 16-byte shared load per staged row and lane) and the four quarters of
+// a warp take four subsets of the level, which all have 2^(m-1) - 1 pairs.
 __device__ void batch_merge(const BatchArgs &a, int32_t *table, int32_t n, int32_t k, int32_t m,
                             const int32_t *terms, int32_t *S)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int ql = lane & 7, nq = nw * 4;
     const int32_t lo_b = xs_start(a, k, 1), lo_e = xs_start(a, k, m);       // rows of size 1..m-1
     const int32_t x_b = xs_start(a, k, m), x_e = xs_start(a, k, m + 1);     // rows of size m
     const uint32_t *xs = a.xs;
+    const uint4 *S4 = reinterpret_cast<const uint4 *>(S) + ql;  // staged row Y, this lane's 4 vertices: S4[Y * 8]
     for (int32_t vb = 0; vb < n; vb += 32) {
         const int32_t v = vb + lane;
         for (int32_t i = lo_b + warp; i < lo_e; i += nw) {
@@ -39,23 +44,39 @@ __device__ void batch_merge(const BatchArgs &a, int32_t *table, int32_t n, int32
             S[Y * 32 + lane] = (v < n) ? table[(int64_t)Y * n + v] : INF;
         }
         __syncthreads();
-        if (v < n) {
-            for (int32_t i = x_b + warp; i < x_e; i += nw) {
-                const uint32_t X = __ldg(xs + i);
-                const uint32_t low = X & (0u - X), rest = X ^ low;
-                uint32_t acc = (uint32_t)INF;
-                uint32_t s = 0;
-                do {
-                    const uint32_t Y = low | s;
-                    acc = min(acc, (uint32_t)S[Y * 32 + lane] + (uint32_t)S[(X ^ Y) * 32 + lane]);
-                    s = (s - rest) & rest;
-                } while (s != rest);
-                for (uint32_t bits = X; bits; bits &= bits - 1) {
-                    const int t = __ffs(bits) - 1;
-                    if (terms[t] == v) acc = (uint32_t)S[(X ^ (1u << t)) * 32 + lane];
-                }
-                table[(int64_t)X * n + v] = (int32_t)acc;
+        for (int32_t i0 = x_b + warp * 4; i0 < x_e; i0 += nq) {
+            const int32_t i = i0 + (lane >> 3);
+            const bool live = i < x_e;
+            const uint32_t X = __ldg(xs + (live ? i : x_b));
+            const uint32_t low = X & (0u - X), rest = X ^ low;
+            uint4 acc = make_uint4((uint32_t)INF, (uint32_t)INF, (uint32_t)INF, (uint32_t)INF);
+            uint32_t sub = 0;
+            do {  // 2^(m-1) - 1 pairs {Y, X\Y}, Y holding X's lowest terminal
+                const uint32_t Y = low | sub;
+                const uint4 y = S4[Y * 8], z = S4[(X ^ Y) * 8];
+                acc.x = min(acc.x, y.x + z.x);
+                acc.y = min(acc.y, y.y + z.y);
+                acc.z = min(acc.z, y.z + z.z);
+                acc.w = min(acc.w, y.w + z.w);
+                sub = (sub - rest) & rest;
+            } while (sub != rest);
+            if (!live) continue;
+            const int32_t v4 = vb + ql * 4;
+            for (uint32_t bits = X; bits; bits &= bits - 1) {  // terminal override (R:2099-2107)
+                const int t = __ffs(bits) - 1;
+                const int32_t d = terms[t] - v4;
+                if (d < 0 || d >= 4) continue;
+                const uint32_t o = (uint32_t)S[(X ^ (1u << t)) * 32 + ql * 4 + d];
+                if (d == 0) acc.x = o;
+                else if (d == 1) acc.y = o;
+                else if (d == 2) acc.z = o;
+                else acc.w = o;
             }
+            int32_t *row = table + (int64_t)X * n + v4;
+            if (v4 < n) row[0] = (int32_t)acc.x;
+            if (v4 + 1 < n) row[1] = (int32_t)acc.y;
+            if (v4 + 2 < n) row[2] = (int32_t)acc.z;
+            if (v4 + 3 < n) row[3] = (int32_t)acc.w;
         }
         __syncthreads();
     }
@@ -155,7 +176,7 @@ __device__ void batch_solve_one(const BatchArgs &a, const BatchInst &I, int32_t 
 // largest first) from a device counter until the queue is empty.
 __global__ void __launch_bounds__(BATCH_THREADS, 1) k_batch(BatchArgs a)
 {
-    extern __shared__ int32_t S[];
+    extern __shared__ __align__(16) int32_t S[];
     __shared__ int32_t s_idx;
     for (;;) {
         if (threadIdx.x == 0) s_idx = (int32_t)atomicAdd(a.queue, 1u);

@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <new>
 #include <numeric>
 #include <vector>
 
@@ -113,10 +114,14 @@ extern "C" int emv_destroy(emv_ctx *c)
     if (!c) return EMV_OK;
     cudaSetDevice(c->device);
     cudaDeviceSynchronize();
-    for (DevBuf *b : {&c->ctrl, &c->stat, &c->scratch, &c->act, &c->adj, &c->xs, &c->mpairs, &c->movr,
-                      &c->mstream_data, &c->mstream_phases, &c->stamp, &c->terms, &c->g_row,
+    for (DevBuf *b : {&c->ctrl, &c->stat, &c->scratch, &c->act, &c->adj, &c->stamp, &c->terms, &c->g_row,
                       &c->g_col, &c->g_w, &c->table, &c->tb_edges, &c->tb_out, &c->tb_work})
         dev_release(*b);
+    for (KPlan *p : c->kplans) {
+        if (!p) continue;
+        for (DevBuf *b : {&p->xs, &p->mpairs, &p->movr, &p->mstream_data, &p->mstream_phases}) dev_release(*b);
+        delete p;
+    }
     for (int i = 0; i < MAX_EVENTS; i++)
         if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     if (c->pinned) cudaFreeHost(c->pinned);
@@ -307,9 +312,9 @@ bool plan_level(const std::vector<uint32_t> &xs, const std::vector<int64_t> &off
 
 int plan_stream_merge(emv_ctx *c, int32_t k, cudaStream_t st)
 {
-    const std::vector<uint32_t> &xs = c->xs_host;
-    const std::vector<int64_t> &off = c->xs_off;
-    c->mstream_groups.assign((size_t)k + 2, {});
+    const std::vector<uint32_t> &xs = c->kp->xs_host;
+    const std::vector<int64_t> &off = c->kp->xs_off;
+    c->kp->mstream_groups.assign((size_t)k + 2, {});
     if (k > MERGE_SMEM_KMAX) return EMV_OK;
     std::vector<uint32_t> rank((size_t)1 << k, 0);  // position within its level
     for (int32_t m = 1; m <= k; m++)
@@ -344,10 +349,10 @@ int plan_stream_merge(emv_ctx *c, int32_t k, cudaStream_t st)
         plan[(size_t)m] = best_groups;
     }
     if (data.empty()) return EMV_OK;
-    int r = dev_reserve(c->mstream_data, sizeof(uint32_t) * data.size());
+    int r = dev_reserve(c->kp->mstream_data, sizeof(uint32_t) * data.size());
     if (r) return r;
     std::vector<MergePhase> phases;
-    const uint32_t *base = (const uint32_t *)c->mstream_data.ptr;
+    const uint32_t *base = (const uint32_t *)c->kp->mstream_data.ptr;
     for (int32_t m = 2; m <= k; m++)
         for (const HostGroup &G : plan[(size_t)m]) {
             StreamGroup sg;
@@ -368,39 +373,67 @@ int plan_stream_merge(emv_ctx *c, int32_t k, cudaStream_t st)
                 mp.pad_ = 0;
                 phases.push_back(mp);
             }
-            c->mstream_groups[(size_t)m].push_back(sg);
+            c->kp->mstream_groups[(size_t)m].push_back(sg);
         }
-    r = dev_reserve(c->mstream_phases, sizeof(MergePhase) * std::max<size_t>(1, phases.size()));
+    r = dev_reserve(c->kp->mstream_phases, sizeof(MergePhase) * std::max<size_t>(1, phases.size()));
     if (r) return r;
-    CUDA_TRY(cudaMemcpyAsync(c->mstream_data.ptr, data.data(), sizeof(uint32_t) * data.size(), cudaMemcpyHostToDevice,
+    CUDA_TRY(cudaMemcpyAsync(c->kp->mstream_data.ptr, data.data(), sizeof(uint32_t) * data.size(), cudaMemcpyHostToDevice,
                              st));
     if (!phases.empty())
-        CUDA_TRY(cudaMemcpyAsync(c->mstream_phases.ptr, phases.data(), sizeof(MergePhase) * phases.size(),
+        CUDA_TRY(cudaMemcpyAsync(c->kp->mstream_phases.ptr, phases.data(), sizeof(MergePhase) * phases.size(),
                                  cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaStreamSynchronize(st));
     return EMV_OK;
 }
 
+static int build_plan(emv_ctx *c, int32_t k, cudaStream_t st);
+
 int prepare_subsets(emv_ctx *c, int32_t k, cudaStream_t st)
 {
     if (c->xs_k == k) return EMV_OK;
-    subset_levels(k, c->xs_host, c->xs_off);
-    int r = dev_reserve(c->xs, sizeof(uint32_t) * std::max<size_t>(1, c->xs_host.size()));
+    if (k < 1 || k > EMV_MAX_K) return emv_fail(EMV_ERR_BAD_INPUT, "k = %d", k);
+    if (c->kplans[k]) {  // built before on this context
+        c->kp = c->kplans[k];
+        c->xs_k = k;
+        return EMV_OK;
+    }
+    KPlan *plan = new (std::nothrow) KPlan();
+    if (!plan) return emv_fail(EMV_ERR_OOM, "plan");
+    c->kp = plan;
+    c->xs_k = -1;
+    const int r0 = build_plan(c, k, st);
+    if (r0) {
+        for (DevBuf *b : {&plan->xs, &plan->mpairs, &plan->movr, &plan->mstream_data, &plan->mstream_phases})
+            dev_release(*b);
+        delete plan;
+        c->kp = nullptr;
+        return r0;
+    }
+    c->kplans[k] = plan;
+    c->xs_k = k;
+    return EMV_OK;
+}
+
+// Builds c->kp for k: subsets, slot lists and the streamed merge plan.
+static int build_plan(emv_ctx *c, int32_t k, cudaStream_t st)
+{
+    subset_levels(k, c->kp->xs_host, c->kp->xs_off);
+    int r = dev_reserve(c->kp->xs, sizeof(uint32_t) * std::max<size_t>(1, c->kp->xs_host.size()));
     if (r) return r;
-    CUDA_TRY(cudaMemcpyAsync(c->xs.ptr, c->xs_host.data(), sizeof(uint32_t) * c->xs_host.size(),
+    CUDA_TRY(cudaMemcpyAsync(c->kp->xs.ptr, c->kp->xs_host.data(), sizeof(uint32_t) * c->kp->xs_host.size(),
                              cudaMemcpyHostToDevice, st));
     // Pair and override slot lists of the shared-memory merge (level order).
-    c->mpair_base.assign((size_t)k + 2, 0);
-    c->movr_base.assign((size_t)k + 2, 0);
+    c->kp->mpair_base.assign((size_t)k + 2, 0);
+    c->kp->movr_base.assign((size_t)k + 2, 0);
     std::vector<uint32_t> pairs, ovr;
     if (k <= MERGE_SMEM_KMAX) {
         std::vector<uint32_t> lidx((size_t)1 << k, 0);
-        for (size_t i = 0; i < c->xs_host.size(); i++) lidx[c->xs_host[i]] = (uint32_t)i;
+        for (size_t i = 0; i < c->kp->xs_host.size(); i++) lidx[c->kp->xs_host[i]] = (uint32_t)i;
         for (int32_t m = 2; m <= k; m++) {
-            c->mpair_base[(size_t)m] = (int64_t)pairs.size();
-            c->movr_base[(size_t)m] = (int64_t)ovr.size();
-            for (int64_t i = c->xs_off[(size_t)m]; i < c->xs_off[(size_t)m + 1]; i++) {
-                const uint32_t X = c->xs_host[(size_t)i];
+            c->kp->mpair_base[(size_t)m] = (int64_t)pairs.size();
+            c->kp->movr_base[(size_t)m] = (int64_t)ovr.size();
+            for (int64_t i = c->kp->xs_off[(size_t)m]; i < c->kp->xs_off[(size_t)m + 1]; i++) {
+                const uint32_t X = c->kp->xs_host[(size_t)i];
                 const uint32_t low = X & (0u - X), rest = X ^ low;
                 uint32_t sm = 0;
                 do {
@@ -416,15 +449,14 @@ int prepare_subsets(emv_ctx *c, int32_t k, cudaStream_t st)
     r = plan_stream_merge(c, k, st);
     if (r) return r;
     if (!pairs.empty()) {
-        r = dev_reserve(c->mpairs, sizeof(uint32_t) * pairs.size());
-        if (!r) r = dev_reserve(c->movr, sizeof(uint32_t) * ovr.size());
+        r = dev_reserve(c->kp->mpairs, sizeof(uint32_t) * pairs.size());
+        if (!r) r = dev_reserve(c->kp->movr, sizeof(uint32_t) * ovr.size());
         if (r) return r;
-        CUDA_TRY(cudaMemcpyAsync(c->mpairs.ptr, pairs.data(), sizeof(uint32_t) * pairs.size(), cudaMemcpyHostToDevice,
+        CUDA_TRY(cudaMemcpyAsync(c->kp->mpairs.ptr, pairs.data(), sizeof(uint32_t) * pairs.size(), cudaMemcpyHostToDevice,
                                  st));
-        CUDA_TRY(cudaMemcpyAsync(c->movr.ptr, ovr.data(), sizeof(uint32_t) * ovr.size(), cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemcpyAsync(c->kp->movr.ptr, ovr.data(), sizeof(uint32_t) * ovr.size(), cudaMemcpyHostToDevice, st));
     }
     CUDA_TRY(cudaStreamSynchronize(st));
-    c->xs_k = k;
     return EMV_OK;
 }
 
@@ -432,14 +464,14 @@ template <int VB>
 static cudaError_t merge_smem_launch(emv_ctx *c, int32_t *table, int64_t ld, int32_t n, int32_t k, int32_t m,
                                      const int32_t *d_terms, cudaStream_t st)
 {
-    const int64_t b = c->xs_off[(size_t)m], cnt = c->xs_off[(size_t)m + 1] - b;
-    const int32_t nstage = (int32_t)c->xs_off[(size_t)m];
-    const uint32_t *xs = (const uint32_t *)c->xs.ptr;
+    const int64_t b = c->kp->xs_off[(size_t)m], cnt = c->kp->xs_off[(size_t)m + 1] - b;
+    const int32_t nstage = (int32_t)c->kp->xs_off[(size_t)m];
+    const uint32_t *xs = (const uint32_t *)c->kp->xs.ptr;
     const size_t smem = sizeof(int32_t) * (size_t)nstage * VB;
     const int32_t npairs = (1 << (m - 1)) - 1;
     k_merge_smem<VB><<<(unsigned)((n + VB - 1) / VB), 1024, smem, st>>>(
-        table, ld, n, xs + b, (int32_t)cnt, xs, nstage, (const uint32_t *)c->mpairs.ptr + c->mpair_base[(size_t)m],
-        npairs, (const uint32_t *)c->movr.ptr + c->movr_base[(size_t)m], m, d_terms);
+        table, ld, n, xs + b, (int32_t)cnt, xs, nstage, (const uint32_t *)c->kp->mpairs.ptr + c->kp->mpair_base[(size_t)m],
+        npairs, (const uint32_t *)c->kp->movr.ptr + c->kp->movr_base[(size_t)m], m, d_terms);
     (void)k;
     return cudaGetLastError();
 }
@@ -459,16 +491,16 @@ int launch_merge(emv_ctx *c, int32_t *table, int64_t ld, int32_t n, int32_t k, i
                                       STREAM_SMEM_BYTES));
         c->merge_attr = true;
     }
-    const int64_t nstage = c->xs_off[(size_t)m];
+    const int64_t nstage = c->kp->xs_off[(size_t)m];
     cudaError_t e = cudaSuccess;
     c->launches++;
-    if (k <= MERGE_SMEM_KMAX && !c->mstream_groups[(size_t)m].empty()) {
-        const int64_t b = c->xs_off[(size_t)m];
-        c->launches += (int64_t)c->mstream_groups[(size_t)m].size() - 1;
-        for (const StreamGroup &g : c->mstream_groups[(size_t)m]) {
+    if (k <= MERGE_SMEM_KMAX && !c->kp->mstream_groups[(size_t)m].empty()) {
+        const int64_t b = c->kp->xs_off[(size_t)m];
+        c->launches += (int64_t)c->kp->mstream_groups[(size_t)m].size() - 1;
+        for (const StreamGroup &g : c->kp->mstream_groups[(size_t)m]) {
             k_merge_stream<<<(unsigned)((n + 31) / 32), 1024, (size_t)g.smem, st>>>(
-                table, ld, n, (const uint32_t *)c->xs.ptr + b + g.x0, (int32_t)g.cnt,
-                (const MergePhase *)c->mstream_phases.ptr + g.phase_off, (int32_t)g.nphase, d_terms, k);
+                table, ld, n, (const uint32_t *)c->kp->xs.ptr + b + g.x0, (int32_t)g.cnt,
+                (const MergePhase *)c->kp->mstream_phases.ptr + g.phase_off, (int32_t)g.nphase, d_terms, k);
             e = cudaGetLastError();
             if (e != cudaSuccess) break;
         }
@@ -481,10 +513,10 @@ int launch_merge(emv_ctx *c, int32_t *table, int64_t ld, int32_t n, int32_t k, i
         else if (row_bytes * 2 <= MERGE_SMEM_BYTES) e = merge_smem_launch<2>(c, table, ld, n, k, m, d_terms, st);
         else e = merge_smem_launch<1>(c, table, ld, n, k, m, d_terms, st);
     } else {
-        const int64_t b = c->xs_off[(size_t)m], cnt = c->xs_off[(size_t)m + 1] - b;
+        const int64_t b = c->kp->xs_off[(size_t)m], cnt = c->kp->xs_off[(size_t)m + 1] - b;
         const int32_t xper = (int32_t)std::min<int64_t>(cnt, 64);
         dim3 grid((unsigned)((n + 31) / 32), (unsigned)((cnt + xper - 1) / xper));
-        k_merge<<<grid, 256, 0, st>>>(table, ld, n, (const uint32_t *)c->xs.ptr + b, (int32_t)cnt, xper, d_terms, k);
+        k_merge<<<grid, 256, 0, st>>>(table, ld, n, (const uint32_t *)c->kp->xs.ptr + b, (int32_t)cnt, xper, d_terms, k);
         e = cudaGetLastError();
     }
     if (e != cudaSuccess) return emv_fail(EMV_ERR_CUDA, "merge launch: %s", cudaGetErrorString(e));
@@ -502,7 +534,7 @@ int run_dp(emv_ctx *c, int32_t n, const int32_t *row_ptr, const int2 *adj, int32
     int32_t *d_terms = (int32_t *)c->terms.ptr;
     CUDA_TRY(cudaMemcpyAsync(d_terms, terms_host, sizeof(int32_t) * (size_t)k, cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemsetAsync(c->stat.ptr, 0, sizeof(DevStat), st));
-    const uint32_t *xs = (const uint32_t *)c->xs.ptr;
+    const uint32_t *xs = (const uint32_t *)c->kp->xs.ptr;
     int ev = 0;
     cudaEvent_t *E = c->ev;
     CUDA_TRY(cudaEventRecord(E[ev++], st));  // 0: start
@@ -513,12 +545,12 @@ int run_dp(emv_ctx *c, int32_t n, const int32_t *row_ptr, const int2 *adj, int32
     CUDA_TRY(cudaEventRecord(E[ev++], st));  // 1: after fill
 
     // Level 1: k single-source closures (R:1988-2031).
-    r = launch_relax(c, row_ptr, adj, n, ld, table, xs + c->xs_off[1], k, d_terms, 1, st);
+    r = launch_relax(c, row_ptr, adj, n, ld, table, xs + c->kp->xs_off[1], k, d_terms, 1, st);
     if (r) return r;
     CUDA_TRY(cudaEventRecord(E[ev++], st));  // 2: after level 1
 
     for (int32_t m = 2; m <= k; m++) {
-        const int64_t b = c->xs_off[(size_t)m], cnt = c->xs_off[(size_t)m + 1] - b;
+        const int64_t b = c->kp->xs_off[(size_t)m], cnt = c->kp->xs_off[(size_t)m + 1] - b;
         r = launch_merge(c, table, ld, n, k, m, d_terms, st);
         if (r) return r;
         CUDA_TRY(cudaEventRecord(E[ev++], st));  // merge end of level m
@@ -777,7 +809,7 @@ extern "C" int emv_sssp(emv_ctx *c, const emv_graph *g, int32_t source, int64_t 
     k_pack_adj<<<grid_for(arcs, 256, 4096), 256, 0, st>>>((const int32_t *)c->g_col.ptr, (const int32_t *)c->g_w.ptr,
                                                           (int2 *)c->adj.ptr, arcs);
     r = launch_relax(c, (const int32_t *)c->g_row.ptr, (const int2 *)c->adj.ptr, n, n, (int32_t *)c->table.ptr,
-                     (const uint32_t *)c->xs.ptr, 1, (const int32_t *)c->terms.ptr, 1, st);
+                     (const uint32_t *)c->kp->xs.ptr, 1, (const int32_t *)c->terms.ptr, 1, st);
     if (r) return r;
     CUDA_TRY(cudaEventRecord(c->ev[1], st));
     std::vector<int32_t> d((size_t)n);

@@ -35,6 +35,19 @@ struct StreamGroup {
     int64_t x0, cnt, phase_off, nphase, smem;
 };
 
+// Everything the DP needs per k, built once per k and context: the subsets by
+// level, the pair and override slots of the staged-all-rows merge and the
+// streamed merge's groups and phases.
+struct KPlan {
+    std::vector<uint32_t> xs_host;
+    std::vector<int64_t> xs_off;   // level m occupies xs[off[m], off[m+1])
+    DevBuf xs;                     // subsets by level
+    DevBuf mpairs, movr;           // merge pair slots and override slots, all levels
+    std::vector<int64_t> mpair_base, movr_base;  // per level
+    DevBuf mstream_data, mstream_phases;
+    std::vector<std::vector<StreamGroup>> mstream_groups;  // per level (none = not streamed)
+};
+
 struct emv_ctx {
     int device = 0;
     int sms = 0;
@@ -45,21 +58,16 @@ struct emv_ctx {
     DevBuf scratch, act;           // vertex-major chunk buffer, active flags
     DevBuf stamp;                  // per vertex: last sweep in which it changed
     DevBuf adj;                    // packed (col, w) arcs
-    DevBuf xs, terms;              // subsets by level, terminals
+    DevBuf terms;                  // terminals
     DevBuf g_row, g_col, g_w;      // device copy of a host CSR
     DevBuf table;                  // DP table of emv_solve
     DevBuf tb_edges, tb_out, tb_work;
     void *pinned = nullptr;        // small pinned host buffer for scalar reads
     cudaEvent_t ev[MAX_EVENTS] = {};
-    int32_t xs_k = -1;             // k of the cached subset list
-    std::vector<uint32_t> xs_host;
-    std::vector<int64_t> xs_off;   // level m occupies xs[off[m], off[m+1])
-    DevBuf mpairs, movr;           // merge pair slots and override slots, all levels of xs_k
-    std::vector<int64_t> mpair_base, movr_base;  // per level
+    int32_t xs_k = -1;             // k of the current plan
+    KPlan *kp = nullptr;           // plan of xs_k
+    KPlan *kplans[EMV_MAX_K + 1] = {};  // plans of every k used so far
     bool merge_attr = false;
-    // streamed merge plan of xs_k: per level, its subset groups (none = not streamed)
-    DevBuf mstream_data, mstream_phases;
-    std::vector<std::vector<StreamGroup>> mstream_groups;
     int64_t launches = 0;
     // batched launch
     DevBuf bxs, bxs_off;           // subset lists of every k <= BATCH_KMAX
