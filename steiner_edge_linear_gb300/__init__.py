@@ -77,6 +77,15 @@ class _Instance(ctypes.Structure):
     _fields_ = [("g", _Graph), ("terminals", ctypes.c_void_p), ("k", ctypes.c_int32)]
 
 
+_INSTANCE_DTYPE = np.dtype({"names": ["n", "arcs", "row_ptr", "col", "w", "terminals", "k"],
+                            "formats": ["<i4", "<i8", "<u8", "<u8", "<u8", "<u8", "<i4"],
+                            "offsets": [_Instance.g.offset + _Graph.n.offset, _Instance.g.offset + _Graph.arcs.offset,
+                                        _Instance.g.offset + _Graph.row_ptr.offset,
+                                        _Instance.g.offset + _Graph.col.offset, _Instance.g.offset + _Graph.w.offset,
+                                        _Instance.terminals.offset, _Instance.k.offset],
+                            "itemsize": ctypes.sizeof(_Instance)})
+
+
 class _BatchStats(ctypes.Structure):
     _fields_ = [("total_ms", ctypes.c_float), ("upload_ms", ctypes.c_float), ("work_items", ctypes.c_int64),
                 ("table_bytes", ctypes.c_int64), ("merge_tile", ctypes.c_int32), ("relax_rows", ctypes.c_int32)]
@@ -282,6 +291,19 @@ class Csr:
         _check(load_library().emv_csr_build(n, m, _ptr(e), _ptr(row), _ptr(col), _ptr(w)))
         return Csr(n, row, col[:2 * m], w[:2 * m], np.ascontiguousarray(g.terminals, dtype=np.int32), g.cost)
 
+    def _ptrs(self) -> tuple:
+        """(n, arcs, row_ptr, col, w, terminals, k) with data addresses, cached
+        while the same array objects stay attached (in-place edits keep them)."""
+        arrays = (self.row_ptr, self.col, self.w, self.terminals)
+        c = self.__dict__.get("_ptr_cache")
+        # the cache holds the array objects themselves, so an identity match is
+        # the same live buffers
+        if c is None or self.n != c[1][0] or any(x is not y for x, y in zip(arrays, c[0])):
+            c = (arrays, (self.n, int(self.col.shape[0]), self.row_ptr.ctypes.data, self.col.ctypes.data,
+                          self.w.ctypes.data, self.terminals.ctypes.data, int(self.terminals.shape[0])))
+            self.__dict__["_ptr_cache"] = c
+        return c[1]
+
     def c_graph(self) -> _Graph:
         return _Graph(self.n, self.arcs, _ptr(self.row_ptr), _ptr(self.col), _ptr(self.w))
 
@@ -450,16 +472,18 @@ class Solver:
 
     @staticmethod
     def _instances(graphs: Sequence[Csr]):
-        insts = (_Instance * len(graphs))()
-        for i, g in enumerate(graphs):
-            insts[i].g = g.c_graph()
-            insts[i].terminals = g.terminals.ctypes.data
-            insts[i].k = g.k
-        return insts
+        """emv_instance array of the graphs, filled column-wise through a numpy
+        view of the same layout (much cheaper than per-field ctypes stores)."""
+        arr = np.zeros(len(graphs), _INSTANCE_DTYPE)
+        if graphs:
+            cols = list(zip(*(g._ptrs() for g in graphs)))
+            for name, col in zip(("n", "arcs", "row_ptr", "col", "w", "terminals", "k"), cols):
+                arr[name] = col
+        return arr.ctypes.data_as(ctypes.POINTER(_Instance)), arr
 
     def batch_autotune(self, graphs: Sequence[Csr], stream: Optional[int] = None) -> np.ndarray:
         """Tunes the batched launch per instance class (emv_batch_autotune); returns the rcap table."""
-        insts = self._instances(graphs)
+        insts, _keep = self._instances(graphs)
         out = np.zeros(BATCH_CLASSES, np.int32)
         _check(self._lib.emv_batch_autotune(self._ctx, insts, len(graphs), out.ctypes.data, stream))
         return out
@@ -477,7 +501,7 @@ class Solver:
     def batch_solve(self, graphs: Sequence[Csr], stream: Optional[int] = None) -> tuple[np.ndarray, dict]:
         """Many independent instances in one persistent launch (emv_batch_solve)."""
         count = len(graphs)
-        insts = self._instances(graphs)
+        insts, _keep = self._instances(graphs)
         costs = np.zeros(count, np.int64)
         st = _BatchStats()
         _check(self._lib.emv_batch_solve(self._ctx, insts, count, costs.ctypes.data, ctypes.byref(st), stream))

@@ -9,10 +9,40 @@
 #include "emv_batch_host.h"
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <string>
+#include <thread>
 #include <vector>
+
+namespace {
+
+// f(i) for i in [0, count) on up to 16 host threads (chunks of 16 indices).
+template <class F> void host_parallel_for(int64_t count, F f)
+{
+    const unsigned hw = std::thread::hardware_concurrency();
+    const int64_t T = std::min<int64_t>({16, (int64_t)(hw ? hw : 1), (count + 63) / 64});
+    if (T <= 1) {
+        for (int64_t i = 0; i < count; i++) f(i);
+        return;
+    }
+    std::atomic<int64_t> next{0};
+    auto work = [&]() {
+        for (;;) {
+            const int64_t i0 = next.fetch_add(16);
+            if (i0 >= count) return;
+            for (int64_t i = i0; i < std::min(count, i0 + 16); i++) f(i);
+        }
+    };
+    std::vector<std::thread> th;
+    for (int64_t t = 1; t < T; t++) th.emplace_back(work);
+    work();
+    for (std::thread &t : th) t.join();
+}
+
+}  // namespace
 
 using namespace emv;
 
@@ -117,20 +147,26 @@ extern "C" int emv_batch_solve(emv_ctx *c, const emv_instance *inst, int32_t cou
     CUDA_TRY(cudaSetDevice(c->device));
     cudaStream_t st = (cudaStream_t)stream;
     const auto t0 = std::chrono::steady_clock::now();
-    for (int32_t i = 0; i < count; i++) {
+    // Admission checks of every instance, in parallel on the host; the first
+    // failing instance (lowest index) is reported.
+    std::vector<int> bad((size_t)count, 0);
+    std::vector<std::string> why((size_t)count);
+    host_parallel_for(count, [&](int64_t i) {
         const emv_instance &I = inst[i];
         int r = emv_graph_validate(&I.g);
-        if (r) return emv_fail(r, "instance %d: %s", i, emv_last_error());
-        if (!batch_fits(I.g.n, I.k))
-            return emv_fail(EMV_ERR_BAD_INPUT, "instance %d: n = %d, k = %d outside the batched range (k <= %d)", i,
-                            I.g.n, I.k, BATCH_KMAX);
-        if (!I.terminals) return emv_fail(EMV_ERR_BAD_INPUT, "instance %d: null terminals", i);
-        for (int32_t t = 0; t < I.k; t++)
-            if (I.terminals[t] < 0 || I.terminals[t] >= I.g.n)
-                return emv_fail(EMV_ERR_BAD_INPUT, "instance %d: terminal out of range", i);
-        r = emv_graph_check(&I.g, nullptr);
-        if (r) return emv_fail(r, "instance %d: %s", i, emv_last_error());
-    }
+        if (!r && !batch_fits(I.g.n, I.k))
+            r = emv_fail(EMV_ERR_BAD_INPUT, "n = %d, k = %d outside the batched range (k <= %d)", I.g.n, I.k, BATCH_KMAX);
+        if (!r && !I.terminals) r = emv_fail(EMV_ERR_BAD_INPUT, "null terminals");
+        for (int32_t t = 0; !r && t < I.k; t++)
+            if (I.terminals[t] < 0 || I.terminals[t] >= I.g.n) r = emv_fail(EMV_ERR_BAD_INPUT, "terminal out of range");
+        if (!r) r = emv_graph_check(&I.g, nullptr);
+        if (r) {
+            bad[(size_t)i] = r;
+            why[(size_t)i] = emv_last_error();
+        }
+    });
+    for (int32_t i = 0; i < count; i++)
+        if (bad[(size_t)i]) return emv_fail(bad[(size_t)i], "instance %d: %s", i, why[(size_t)i].c_str());
     // Largest first, so the persistent CTAs finish together.
     std::vector<int32_t> order((size_t)count);
     for (int32_t i = 0; i < count; i++) order[(size_t)i] = i;
@@ -222,13 +258,13 @@ int batch_pack(emv_ctx *c, const emv_instance *inst, const std::vector<int32_t> 
     int2 *hadj = (int2 *)(hrow + rows);
     int32_t *hterm = (int32_t *)(hadj + arcs);
     BatchInst *hdesc = (BatchInst *)(((uintptr_t)(hterm + terms) + 15) & ~(uintptr_t)15);
-    for (int32_t j = 0; j < count; j++) {
+    host_parallel_for(count, [&](int64_t j) {  // disjoint ranges of the staging buffer
         const emv_instance &I = inst[order[(size_t)j]];
         std::memcpy(hrow + pk.row_off[(size_t)j], I.g.row_ptr, sizeof(int32_t) * ((size_t)I.g.n + 1));
         int2 *ha = hadj + pk.arc_off[(size_t)j];
         for (int64_t e = 0; e < I.g.arcs; e++) ha[e] = make_int2(I.g.col[e], I.g.w[e]);
         std::memcpy(hterm + pk.term_off[(size_t)j], I.terminals, sizeof(int32_t) * (size_t)I.k);
-    }
+    });
     std::memcpy(hdesc, pk.desc.data(), sizeof(BatchInst) * (size_t)count);
     pk.h_row = hrow;
     pk.h_adj = hadj;
