@@ -16,6 +16,7 @@
 
 #include "emv_batch_types.h"
 #include "emv_common.cuh"
+#include "emv_device_util.cuh"
 
 namespace emv {
 
@@ -39,10 +40,13 @@ __device__ void batch_merge(const BatchArgs &a, int32_t *table, int32_t n, int32
     const uint4 *S4 = reinterpret_cast<const uint4 *>(S) + ql;  // staged row Y, this lane's 4 vertices: S4[Y * 8]
     for (int32_t vb = 0; vb < n; vb += 32) {
         const int32_t v = vb + lane;
+        // staging: 4-byte asynchronous copies, so a warp has all its rows in flight
         for (int32_t i = lo_b + warp; i < lo_e; i += nw) {
             const uint32_t Y = __ldg(xs + i);
-            S[Y * 32 + lane] = (v < n) ? table[(int64_t)Y * n + v] : INF;
+            if (v < n) cp_async4(S + Y * 32 + lane, table + (int64_t)Y * n + v);
+            else S[Y * 32 + lane] = INF;
         }
+        cp_async_wait_all();
         __syncthreads();
         for (int32_t i0 = x_b + warp * 4; i0 < x_e; i0 += nq) {
             const int32_t i = i0 + (lane >> 3);

@@ -43,6 +43,15 @@ __device__ __forceinline__ bool grid_barrier(uint32_t *ctrl, int *s_ok)
     return *s_ok != 0;
 }
 
+// 4-byte asynchronous global -> shared copy (staging without a register round
+// trip) and the wait for all of this thread's copies.
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)), "l"(gmem)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // Vector of VEC int32 (one lane's share of a vertex record).
 template <int VEC> struct IVec;
 template <> struct IVec<1> {

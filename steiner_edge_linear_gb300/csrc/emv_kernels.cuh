@@ -197,12 +197,6 @@ struct MergePhase {
 // several quarters; partial minima meet in acc through shared-memory
 // atomicMin.  The terminal override of the virtual-source arcs
 // (R:2099-2107) is applied last, from the finished level m-1 rows.
-__device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
-{
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)), "l"(gmem)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 __device__ __forceinline__ void merge_pair4(uint4 &a, const uint4 *__restrict__ S4, uint32_t pr)
 {
