@@ -304,9 +304,7 @@ def run_single(args, dist: Dist, cfg: dict = SINGLE, cfg_name: str = SINGLE_NAME
            "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": round(ms / args.steps, 3),
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
            "data": "synthetic (seeded generator, configuration-model random regular graph)",
-           "config": {"workload": cfg_name, "n": n, "m": m, "k": k, "table_bytes": 4 * n << k,
-                      "parallelism": f"replicas x{dist.world}",
-                      "l2": f"no flush: {4 * (n << k) / 1e9:.1f} GB table per step > 129 MB L2"},
+           "config": single_config(cfg, cfg_name, dist.world),
            "cost": cost,
            "e2e": {"value": round(args.steps * dist.world / e2e_s, 4), "unit": "solves/s",
                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -330,6 +328,14 @@ def run_single(args, dist: Dist, cfg: dict = SINGLE, cfg_name: str = SINGLE_NAME
     return out
 
 
+def single_config(cfg: dict, name: str, world: int) -> dict:
+    """The `config` object of a single-solve line (both arms)."""
+    n, k = cfg["n"], cfg["k"]
+    return {"workload": name, "n": n, "m": n * cfg["degree"] // 2, "k": k, "table_bytes": 4 * n << k,
+            "parallelism": f"replicas x{world}",
+            "l2": f"no flush: {4 * (n << k) / 1e9:.1f} GB table per step > 129 MB L2"}
+
+
 def run_reference(args, dist: Dist) -> dict | None:
     """The reference arm: each timed step is one complete solve of the benchmark
     instance by the reference's own emv_kernel on all host cores (about 20 s on
@@ -339,11 +345,12 @@ def run_reference(args, dist: Dist) -> dict | None:
     c = cpu_reference_runs(steps=args.steps, warmup=args.warmup)
     t = statistics.median(c["runs_s"])
     value = 1.0 / t
-    return {"metric": "solves/s", "value": round(value, 5), "unit": "solves/s", "n_gpus": 0, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": round(1000.0 * t, 1), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "int64", "data": "synthetic",
+    return {"metric": "solves/s", "value": round(value, 5), "unit": "solves/s", "n_gpus": dist.world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000.0 * t, 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int64",
+            "data": "synthetic (seeded generator, configuration-model random regular graph)",
             "impl": "reference",
-            "config": {"workload": SINGLE_NAME, "n": SINGLE["n"], "k": SINGLE["k"]},
+            "config": single_config(SINGLE, SINGLE_NAME, dist.world),
             "cpu_baseline": {"value": round(value, 5), "unit": "solves/s", "cores": c["threads"], "kind": c["kind"],
                              "sample": "complete solves of the benchmark instance, median of the timed steps"},
             "e2e": {"value": round(value, 5), "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
