@@ -68,7 +68,7 @@ int32_t batch_class_of(int32_t n, int32_t k)
 int32_t batch_rcap_max(int32_t n)
 {
     int32_t r = 32;
-    while (r > 1 && (int64_t)n * (r + 1) * 4 > BATCH_SMEM_BYTES) r /= 2;
+    while (r > 1 && (int64_t)n * batch_stride(r) * 4 > BATCH_SMEM_BYTES) r /= 2;
     return r;
 }
 

@@ -8,7 +8,7 @@
 //             memory as S[Y][32], a quarter-warp computes one subset X at a
 //             time with 4 vertices per lane (R:2068-2107);
 //   relax  -- chunks of R rows are loaded into shared memory vertex-major
-//             (stride R+1, conflict-free), and in-place sweeps pull
+//             (stride R+1, or R+4 with 4 rows per lane), and in-place sweeps pull
 //             min(d[u] + w) over the CSR until a sweep changes nothing
 //             (R:2109-2130), then the rows go back to the table.
 // The table of an instance is int32 row-major with ld = n.
@@ -95,9 +95,13 @@ __device__ bool batch_relax(const BatchArgs &a, int32_t *table, int32_t n, const
     const int32_t cnt = e - b;
     int32_t R = 1;
     while (R < cnt && R < rcap) R <<= 1;
-    const int32_t stride = R + 1;
-    const int32_t G = 32 / R;              // vertices per warp task
-    const int32_t vs = lane / R, r = lane % R;
+    const int32_t stride = batch_stride(R);
+    // R >= 4: a lane holds 4 consecutive rows of a vertex (16-byte shared loads);
+    // else a lane holds one row
+    const int32_t RV = R >= 4 ? 4 : 1;
+    const int32_t LPV = R / RV;            // lanes per vertex
+    const int32_t G = 32 / LPV;            // vertices per warp task
+    const int32_t vs = lane / LPV, r = (lane % LPV) * RV;
     bool ok = true;
     for (int32_t c0 = 0; c0 < cnt; c0 += R) {
         const int32_t nr = min(R, cnt - c0);
@@ -118,8 +122,21 @@ __device__ bool batch_relax(const BatchArgs &a, int32_t *table, int32_t n, const
             bool changed = false;
             for (int32_t t = warp; t < tasks; t += nw) {
                 const int32_t v = t * G + vs;
-                if (v < n && r < nr) {
-                    const int32_t beg = __ldg(row_ptr + v), end = __ldg(row_ptr + v + 1);
+                if (v >= n || r >= nr) continue;
+                const int32_t beg = __ldg(row_ptr + v), end = __ldg(row_ptr + v + 1);
+                if (RV == 4) {  // rows r..r+3 (rows past nr are INF and never written back)
+                    int4 *mine = reinterpret_cast<int4 *>(S + v * stride + r);
+                    const int4 old = *mine;
+                    int4 acc = old;
+                    for (int32_t q = beg; q < end; q++) {
+                        const int2 arc = __ldg(adj + q);
+                        acc = vmin(acc, vadd(*reinterpret_cast<const int4 *>(S + arc.x * stride + r), arc.y));
+                    }
+                    if (vlt(acc, old)) {
+                        *mine = acc;
+                        changed = true;
+                    }
+                } else {
                     const int32_t old = S[v * stride + r];
                     int32_t acc = old;
                     for (int32_t q = beg; q < end; q++) {

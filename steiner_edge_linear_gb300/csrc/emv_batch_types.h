@@ -9,6 +9,10 @@ namespace emv {
 constexpr int BATCH_THREADS = 1024;
 constexpr int BATCH_KMAX = 12;
 constexpr int32_t BATCH_SMEM_BYTES = 200 * 1024;
+// Shared-memory stride of a vertex in a relaxation chunk of R rows: R + 1
+// (conflict-free single-row lanes) or, for R >= 4, R + 4 (16-byte aligned
+// 4-row lane shares).
+__host__ __device__ constexpr int32_t batch_stride(int32_t R) { return R >= 4 ? R + 4 : R + 1; }
 
 struct BatchInst {
     const int32_t *row_ptr;  // n + 1 entries, arcs of this instance from 0
