@@ -422,7 +422,10 @@ static int build_plan(emv_ctx *c, int32_t k, cudaStream_t st)
     if (r) return r;
     CUDA_TRY(cudaMemcpyAsync(c->kp->xs.ptr, c->kp->xs_host.data(), sizeof(uint32_t) * c->kp->xs_host.size(),
                              cudaMemcpyHostToDevice, st));
-    // Pair and override slot lists of the shared-memory merge (level order).
+    r = plan_stream_merge(c, k, st);
+    if (r) return r;
+    // Pair and override slot lists of the staged-all-rows merge, for the levels
+    // the streamed merge has no plan for (level order).
     c->kp->mpair_base.assign((size_t)k + 2, 0);
     c->kp->movr_base.assign((size_t)k + 2, 0);
     std::vector<uint32_t> pairs, ovr;
@@ -432,6 +435,7 @@ static int build_plan(emv_ctx *c, int32_t k, cudaStream_t st)
         for (int32_t m = 2; m <= k; m++) {
             c->kp->mpair_base[(size_t)m] = (int64_t)pairs.size();
             c->kp->movr_base[(size_t)m] = (int64_t)ovr.size();
+            if (!c->kp->mstream_groups[(size_t)m].empty()) continue;
             for (int64_t i = c->kp->xs_off[(size_t)m]; i < c->kp->xs_off[(size_t)m + 1]; i++) {
                 const uint32_t X = c->kp->xs_host[(size_t)i];
                 const uint32_t low = X & (0u - X), rest = X ^ low;
@@ -446,8 +450,6 @@ static int build_plan(emv_ctx *c, int32_t k, cudaStream_t st)
             }
         }
     }
-    r = plan_stream_merge(c, k, st);
-    if (r) return r;
     if (!pairs.empty()) {
         r = dev_reserve(c->kp->mpairs, sizeof(uint32_t) * pairs.size());
         if (!r) r = dev_reserve(c->kp->movr, sizeof(uint32_t) * ovr.size());

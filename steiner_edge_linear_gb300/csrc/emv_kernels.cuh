@@ -452,32 +452,37 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
 
 // Phase A of a relaxation chunk: rows -> vertex-major records (vertex v owns
 // 32*VEC int32, element e = row e); in level-1 mode the rows are the k
-// single-source initialisations.  Also resets the active flags and stamps.
+// single-source initialisations.  A tile is 32 vertices by all 32*VEC rows,
+// so a warp has all its 2*VEC row loads in flight before one barrier.  Also
+// resets the active flags and stamps.
 template <int VEC>
 __device__ void relax_load_records(const RelaxArgs &a, int32_t (*tile)[33])
 {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwb = blockDim.x >> 5;
+    constexpr int R = 32 * VEC, NW = RELAX_THREADS / 32, PER = R / NW;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int32_t n = a.n, ntiles = (n + 31) >> 5, nrows = a.nrows;
-    constexpr int R = 32 * VEC;
     for (int32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int32_t v = t * 32 + lane;
-        for (int g = 0; g < VEC; g++) {
-            for (int r = warp; r < 32; r += nwb) {
-                const int32_t row = g * 32 + r;
-                int32_t x = INF;
-                if (row < nrows && v < n) {
-                    if (a.level1) x = (v == __ldg(a.terms + row)) ? 0 : INF;
-                    else x = __ldcg(a.table + (int64_t)__ldg(a.rows + row) * a.ld + v);
-                }
-                tile[r][lane] = x;
+        int32_t x[PER];
+#pragma unroll
+        for (int q = 0; q < PER; q++) {
+            const int32_t row = warp + q * NW;
+            x[q] = INF;
+            if (row < nrows && v < n) {
+                if (a.level1) x[q] = (v == __ldg(a.terms + row)) ? 0 : INF;
+                else x[q] = __ldcg(a.table + (int64_t)__ldg(a.rows + row) * a.ld + v);
             }
-            __syncthreads();
-            for (int vv = warp; vv < 32; vv += nwb) {
-                const int32_t v2 = t * 32 + vv;
-                if (v2 < n) __stcg(a.scratch + (int64_t)v2 * R + g * 32 + lane, tile[lane][vv]);
-            }
-            __syncthreads();
         }
+#pragma unroll
+        for (int q = 0; q < PER; q++) tile[warp + q * NW][lane] = x[q];
+        __syncthreads();
+        for (int vv = warp; vv < 32; vv += NW) {
+            const int32_t v2 = t * 32 + vv;
+            if (v2 < n)
+#pragma unroll
+                for (int g = 0; g < VEC; g++) __stcg(a.scratch + (int64_t)v2 * R + g * 32 + lane, tile[g * 32 + lane][vv]);
+        }
+        __syncthreads();
     }
     for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
         a.act0[v] = 1;
@@ -486,28 +491,29 @@ __device__ void relax_load_records(const RelaxArgs &a, int32_t (*tile)[33])
     }
 }
 
-// Phase C: vertex-major records -> table rows.
+// Phase C: vertex-major records -> table rows, a whole 32-vertex tile at a time.
 template <int VEC>
 __device__ void relax_store_records(const RelaxArgs &a, int32_t (*tile)[33])
 {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwb = blockDim.x >> 5;
+    constexpr int R = 32 * VEC, NW = RELAX_THREADS / 32, PER = R / NW;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int32_t n = a.n, ntiles = (n + 31) >> 5, nrows = a.nrows;
-    constexpr int R = 32 * VEC;
     for (int32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        for (int g = 0; g < VEC; g++) {
-            for (int vv = warp; vv < 32; vv += nwb) {
-                const int32_t v2 = t * 32 + vv;
-                tile[vv][lane] = (v2 < n) ? __ldcg(a.scratch + (int64_t)v2 * R + g * 32 + lane) : INF;
-            }
-            __syncthreads();
-            const int32_t v = t * 32 + lane;
-            if (v < n)
-                for (int r = warp; r < 32; r += nwb) {
-                    const int32_t row = g * 32 + r;
-                    if (row < nrows) a.table[(int64_t)__ldg(a.rows + row) * a.ld + v] = tile[lane][r];
-                }
-            __syncthreads();
+        for (int vv = warp; vv < 32; vv += NW) {
+            const int32_t v2 = t * 32 + vv;
+#pragma unroll
+            for (int g = 0; g < VEC; g++)
+                tile[g * 32 + lane][vv] = (v2 < n) ? __ldcg(a.scratch + (int64_t)v2 * R + g * 32 + lane) : INF;
         }
+        __syncthreads();
+        const int32_t v = t * 32 + lane;
+        if (v < n)
+#pragma unroll
+            for (int q = 0; q < PER; q++) {
+                const int32_t row = warp + q * NW;
+                if (row < nrows) a.table[(int64_t)__ldg(a.rows + row) * a.ld + v] = tile[row][lane];
+            }
+        __syncthreads();
     }
 }
 
@@ -521,7 +527,7 @@ __device__ void relax_store_records(const RelaxArgs &a, int32_t (*tile)[33])
 template <int VEC>
 __global__ void __launch_bounds__(RELAX_THREADS, 2) k_relax(RelaxArgs a)
 {
-    __shared__ int32_t tile[32][33];
+    __shared__ int32_t tile[32 * VEC][33];  // 32 vertices by all rows of the chunk
     __shared__ int s_ok;
     relax_load_records<VEC>(a, tile);
     if (!grid_barrier(a.ctrl, &s_ok)) {
