@@ -166,6 +166,12 @@ typedef struct emv_ctx emv_ctx;
  * scratch (relaxation buffers, traceback stack) and grows it on demand. */
 int emv_create(emv_ctx **ctx, int32_t device);
 int emv_destroy(emv_ctx *ctx);
+/* Caps the relaxation sweeps per chunk of the context's later solves (0, the
+ * default, is the Bellman-Ford bound n + 1, which no closure reaches).  A solve
+ * that hits a smaller cap returns EMV_ERR_TIMEOUT and leaves the context
+ * usable: a latency bound for callers that prefer an error to an unusually
+ * long solve.  No reference counterpart (its Dijkstra has no budget). */
+int emv_set_sweep_limit(emv_ctx *ctx, int64_t limit);
 
 /* Per-phase device times of the last solve (CUDA events, ms). */
 typedef struct emv_timing {

@@ -125,6 +125,7 @@ SIGNATURES = {
     "emv_gen_clique": (ctypes.c_int, [_I64, _I32, _I32, _I32, _U64, ctypes.POINTER(ctypes.POINTER(_Stp))]),
     "emv_create": (ctypes.c_int, [ctypes.POINTER(_P), _I32]),
     "emv_destroy": (ctypes.c_int, [_P]),
+    "emv_set_sweep_limit": (ctypes.c_int, [_P, _I64]),
     "emv_kernel_dev": (ctypes.c_int, [_P, _I32, _I64, _P, _P, _P, _I32, _P, _P, _I64, ctypes.POINTER(_I64), _P]),
     "emv_solve": (ctypes.c_int, [_P, ctypes.POINTER(_Graph), _P, _I32, _I32, ctypes.POINTER(_Result), _P]),
     "emv_solve_dev": (ctypes.c_int, [_P, ctypes.POINTER(_Graph), _P, _I32, _I32, ctypes.POINTER(_Result), _P]),
@@ -452,6 +453,11 @@ class Solver:
                                        TREE if tree else 0, ctypes.byref(res), stream))
         tr = tree_buf[:res.tree_count].copy() if tree_buf is not None else None
         return Result(int(res.cost), tr, int(res.tree_weight), None, _timing(res.timing))
+
+    def set_sweep_limit(self, limit: int) -> None:
+        """Caps the relaxation sweeps per chunk (0 = the Bellman-Ford bound); a
+        solve that hits the cap raises EmvError with EMV_ERR_TIMEOUT."""
+        _check(self._lib.emv_set_sweep_limit(self._ctx, int(limit)))
 
     def kernel_dev(self, n: int, arcs: int, row_ptr: int, col: int, w: int, terminals: Sequence[int],
                    table: int, ld: int, stream: Optional[int] = None) -> int:

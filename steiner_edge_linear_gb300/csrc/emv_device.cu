@@ -109,6 +109,13 @@ extern "C" int emv_create(emv_ctx **out, int32_t device)
     return EMV_OK;
 }
 
+extern "C" int emv_set_sweep_limit(emv_ctx *c, int64_t limit)
+{
+    if (!c || limit < 0) return emv_fail(EMV_ERR_BAD_INPUT, "emv_set_sweep_limit: bad arguments");
+    c->sweep_limit = limit;
+    return EMV_OK;
+}
+
 extern "C" int emv_destroy(emv_ctx *c)
 {
     if (!c) return EMV_OK;
@@ -158,7 +165,7 @@ int launch_relax(emv_ctx *c, const int32_t *row_ptr, const int2 *adj, int32_t n,
     a.act1 = (uint8_t *)c->act.ptr + ((size_t)n + 255) / 256 * 256;
     a.ctrl = (uint32_t *)c->ctrl.ptr;
     a.stat = (DevStat *)c->stat.ptr;
-    a.max_sweeps = n + 1;
+    a.max_sweeps = (c->sweep_limit > 0 && c->sweep_limit < (int64_t)n + 1) ? (int32_t)c->sweep_limit : n + 1;
     // Dense sweeps pay off while almost every vertex has a changed neighbour:
     // with mean degree d and a fraction f of vertices changed, a vertex has none
     // with probability (1 - f)^d; take every vertex while that is below 10 %.

@@ -53,6 +53,7 @@ struct emv_ctx {
     int sms = 0;
     int relax_blocks_max[4] = {0, 0, 0, 0};  // cooperative grid of k_relax<1>, <2>, <4>, <8>
     int64_t l2_bytes = 0;
+    int64_t sweep_limit = 0;       // relaxation sweeps per chunk, 0 = n + 1
     int64_t relax_arcs = 0;       // arcs of the graph being relaxed (dense-sweep threshold)
     DevBuf ctrl, stat;             // relaxation barrier words, solve status
     DevBuf scratch, act;           // vertex-major chunk buffer, active flags

@@ -152,6 +152,41 @@ def test_bad_inputs_report_status(emv, solver):
     assert solver.solve(csr).cost > 0
 
 
+def test_sweep_limit_is_a_timeout_status_and_context_survives(emv, orc):
+    """A bounded device loop that runs out reports EMV_ERR_TIMEOUT through the
+    status word; nothing traps and the same context solves again."""
+    inst = emv.StpInstance.regular(3000, 4, 1, 1000, 6, 99)
+    csr = emv.Csr.from_stp(inst)
+    want = orc.emv_table(csr.n, csr.row_ptr, csr.col, csr.w, csr.terminals)[1]
+    with emv.Solver(0) as s:
+        s.set_sweep_limit(2)
+        with pytest.raises(emv.EmvError) as ei:
+            s.solve(csr)
+        assert ei.value.status == 5  # EMV_ERR_TIMEOUT
+        s.set_sweep_limit(0)
+        assert s.solve(csr).cost == want
+        with pytest.raises(emv.EmvError):
+            s.set_sweep_limit(-1)
+
+
+def test_table_beyond_device_memory_is_oom_and_context_survives(emv, solver):
+    """A table larger than the device (n * 2^k * 4 bytes well above its memory)
+    fails its allocation with EMV_ERR_OOM; the context is usable afterwards."""
+    torch = pytest.importorskip("torch")
+    total = torch.cuda.get_device_properties(0).total_memory
+    k = 20
+    n = 1 << 14
+    while n * (4 << k) < 2 * total:
+        n <<= 1
+    inst = emv.StpInstance.regular(n, 4, 1, 10, k, 5)
+    csr = emv.Csr.from_stp(inst)
+    with pytest.raises(emv.EmvError) as ei:
+        solver.solve(csr)
+    assert ei.value.status == 3  # EMV_ERR_OOM
+    small = emv.Csr.from_stp(emv.StpInstance.regular(500, 4, 1, 10, 5, 5))
+    assert solver.solve(small).cost > 0
+
+
 def test_cli_reference_lines(emv, tmp_path):
     """reader-el-gpu -el -list prints the reference's lines; the regexes are
     those of the reference's scripts (experiments/verify.py:126-147)."""
