@@ -105,14 +105,25 @@ __device__ bool batch_relax(const BatchArgs &a, int32_t *table, int32_t n, const
     bool ok = true;
     for (int32_t c0 = 0; c0 < cnt; c0 += R) {
         const int32_t nr = min(R, cnt - c0);
-        for (int32_t idx = threadIdx.x; idx < R * n; idx += blockDim.x) {
-            const int32_t rr = idx / n, v = idx - rr * n;
-            int32_t x = INF;
-            if (rr < nr) {
-                if (level1) x = (v == terms[c0 + rr]) ? 0 : INF;
-                else x = table[(int64_t)__ldg(a.xs + b + c0 + rr) * n + v];
+        auto row_in = [&](int32_t rr, int32_t v) -> int32_t {
+            if (rr >= nr) return INF;
+            if (level1) return (v == terms[c0 + rr]) ? 0 : INF;
+            return table[(int64_t)__ldg(a.xs + b + c0 + rr) * n + v];
+        };
+        if (RV == 4) {
+            // a thread moves 4 rows of one vertex (one 16-byte shared store; with a
+            // stride of R + 4 the 8 lanes of a store phase hit distinct banks)
+            for (int32_t idx = threadIdx.x; idx < (R / 4) * n; idx += blockDim.x) {
+                const int32_t g = idx / n, v = idx - g * n;
+                const int4 x = make_int4(row_in(4 * g, v), row_in(4 * g + 1, v), row_in(4 * g + 2, v),
+                                         row_in(4 * g + 3, v));
+                *reinterpret_cast<int4 *>(S + v * stride + 4 * g) = x;
             }
-            S[v * stride + rr] = x;
+        } else {
+            for (int32_t idx = threadIdx.x; idx < R * n; idx += blockDim.x) {
+                const int32_t rr = idx / n, v = idx - rr * n;
+                S[v * stride + rr] = row_in(rr, v);
+            }
         }
         __syncthreads();
         const int32_t tasks = (n + G - 1) / G;
@@ -151,9 +162,21 @@ __device__ bool batch_relax(const BatchArgs &a, int32_t *table, int32_t n, const
             }
             if (!__syncthreads_or(changed)) break;
         }
-        for (int32_t idx = threadIdx.x; idx < nr * n; idx += blockDim.x) {
-            const int32_t rr = idx / n, v = idx - rr * n;
-            table[(int64_t)__ldg(a.xs + b + c0 + rr) * n + v] = S[v * stride + rr];
+        if (RV == 4) {
+            for (int32_t idx = threadIdx.x; idx < ((nr + 3) / 4) * n; idx += blockDim.x) {
+                const int32_t g = idx / n, v = idx - g * n;
+                const int4 x = *reinterpret_cast<const int4 *>(S + v * stride + 4 * g);
+                const int32_t r0 = 4 * g;
+                table[(int64_t)__ldg(a.xs + b + c0 + r0) * n + v] = x.x;
+                if (r0 + 1 < nr) table[(int64_t)__ldg(a.xs + b + c0 + r0 + 1) * n + v] = x.y;
+                if (r0 + 2 < nr) table[(int64_t)__ldg(a.xs + b + c0 + r0 + 2) * n + v] = x.z;
+                if (r0 + 3 < nr) table[(int64_t)__ldg(a.xs + b + c0 + r0 + 3) * n + v] = x.w;
+            }
+        } else {
+            for (int32_t idx = threadIdx.x; idx < nr * n; idx += blockDim.x) {
+                const int32_t rr = idx / n, v = idx - rr * n;
+                table[(int64_t)__ldg(a.xs + b + c0 + rr) * n + v] = S[v * stride + rr];
+            }
         }
         __syncthreads();
         if (!ok) break;
