@@ -67,7 +67,7 @@ int32_t batch_class_of(int32_t n, int32_t k)
 // Largest rows-per-chunk whose vertex-major buffer fits the shared memory.
 int32_t batch_rcap_max(int32_t n)
 {
-    int32_t r = 32;
+    int32_t r = BATCH_RCAP_MAX;
     while (r > 1 && (int64_t)n * batch_stride(r) * 4 > BATCH_SMEM_BYTES) r /= 2;
     return r;
 }
@@ -379,7 +379,7 @@ extern "C" int emv_batch_autotune(emv_ctx *c, const emv_instance *inst, int32_t 
         if (ids.empty()) continue;
         float best_ms = 1e30f;
         int32_t best = 0;
-        for (int32_t cand : {4, 8, 16, 32}) {
+        for (int32_t cand : {4, 8, 16, 32, 64, 128}) {
             c->tune_rcap[cls] = cand;
             BatchPack pk;
             int r = batch_pack(c, inst, ids, 1, -1, pk);

@@ -9,6 +9,7 @@ namespace emv {
 constexpr int BATCH_THREADS = 1024;
 constexpr int BATCH_KMAX = 12;
 constexpr int32_t BATCH_SMEM_BYTES = 200 * 1024;
+constexpr int32_t BATCH_RCAP_MAX = 128;  // most rows per relaxation chunk (a lane holds 4 of them)
 // Shared-memory stride of a vertex in a relaxation chunk of R rows: R + 1
 // (conflict-free single-row lanes) or, for R >= 4, R + 4 (16-byte aligned
 // 4-row lane shares).

@@ -33,7 +33,7 @@ def test_batch_repeat_and_autotune(emv, mixed):
         table = s.batch_autotune(mixed)
         c, st = s.batch_solve(mixed)
     assert np.array_equal(a, b) and np.array_equal(a, c)
-    assert set(int(x) for x in table) <= {0, 4, 8, 16, 32} and table.max() > 0
+    assert set(int(x) for x in table) <= {0, 4, 8, 16, 32, 64, 128} and table.max() > 0
 
 
 def test_batch_group_instances(emv, orc):
