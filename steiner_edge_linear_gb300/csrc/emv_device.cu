@@ -87,20 +87,26 @@ extern "C" int emv_create(emv_ctx **out, int32_t device)
     c->device = device;
     c->sms = prop.multiProcessorCount;
     c->l2_bytes = prop.l2CacheSize;
-    const void *relax_fns[4] = {(const void *)k_relax<1>, (const void *)k_relax<2>, (const void *)k_relax<4>,
-                                (const void *)k_relax<8>};
-    for (int i = 0; i < 4; i++) {
+    const void *relax_fns[8] = {(const void *)k_relax<1>,       (const void *)k_relax<2>,
+                                (const void *)k_relax<4>,       (const void *)k_relax<8>,
+                                (const void *)k_relax<1, true>, (const void *)k_relax<2, true>,
+                                (const void *)k_relax<4, true>, (const void *)k_relax<8, true>};
+    for (int i = 0; i < 8; i++) {
         int per_sm = 0;
         CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, relax_fns[i], RELAX_THREADS, 0));
         c->relax_blocks_max[i] = std::max(1, per_sm) * c->sms;
     }
     int st = dev_reserve(c->ctrl, sizeof(uint32_t) * C_WORDS);
     if (!st) st = dev_reserve(c->stat, sizeof(DevStat));
+    if (!st) st = dev_reserve(c->lvlmax, sizeof(uint32_t) * (EMV_MAX_K + 1));
     if (!st) {
         if (cudaMallocHost(&c->pinned, 4096) != cudaSuccess) { cudaGetLastError(); st = emv_fail(EMV_ERR_OOM, "pinned"); }
     }
     for (int i = 0; !st && i < MAX_EVENTS; i++)
         if (cudaEventCreate(&c->ev[i]) != cudaSuccess) st = emv_fail(EMV_ERR_CUDA, "event create");
+    for (int i = 0; !st && i <= EMV_MAX_K; i++)
+        if (cudaEventCreateWithFlags(&c->evmax[i], cudaEventDisableTiming) != cudaSuccess)
+            st = emv_fail(EMV_ERR_CUDA, "event create");
     if (st) {
         emv_destroy(c);
         return st;
@@ -116,12 +122,19 @@ extern "C" int emv_set_sweep_limit(emv_ctx *c, int64_t limit)
     return EMV_OK;
 }
 
+extern "C" int emv_set_relax_records(emv_ctx *c, int32_t bits)
+{
+    if (!c || (bits != 0 && bits != 32)) return emv_fail(EMV_ERR_BAD_INPUT, "emv_set_relax_records: bits 0 or 32");
+    c->relax_bits = bits;
+    return EMV_OK;
+}
+
 extern "C" int emv_destroy(emv_ctx *c)
 {
     if (!c) return EMV_OK;
     cudaSetDevice(c->device);
     cudaDeviceSynchronize();
-    for (DevBuf *b : {&c->ctrl, &c->stat, &c->scratch, &c->act, &c->adj, &c->stamp, &c->terms, &c->g_row,
+    for (DevBuf *b : {&c->ctrl, &c->stat, &c->lvlmax, &c->scratch, &c->act, &c->adj, &c->stamp, &c->terms, &c->g_row,
                       &c->g_col, &c->g_w, &c->table, &c->tb_edges, &c->tb_out, &c->tb_work})
         dev_release(*b);
     for (KPlan *p : c->kplans) {
@@ -131,6 +144,8 @@ extern "C" int emv_destroy(emv_ctx *c)
     }
     for (int i = 0; i < MAX_EVENTS; i++)
         if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+    for (int i = 0; i <= EMV_MAX_K; i++)
+        if (c->evmax[i]) cudaEventDestroy(c->evmax[i]);
     if (c->pinned) cudaFreeHost(c->pinned);
     delete c;
     return EMV_OK;
@@ -144,10 +159,14 @@ static int grid_for(int64_t work, int threads, int cap)
     return (int)std::max<int64_t>(1, std::min<int64_t>(g, cap));
 }
 
-// Launches the relaxation of one chunk of at most CHUNK_ROWS rows
-// (cooperative, persistent); the record width follows the row count.
+// Launches the relaxation of one chunk of at most CHUNK_ROWS rows (2 *
+// CHUNK_ROWS with 16-bit records, which the caller takes only for rows whose
+// values are all at most 32767) as one cooperative, persistent kernel; the
+// record width follows the row count.  vmax (or null) receives the largest
+// value written.
 int launch_relax(emv_ctx *c, const int32_t *row_ptr, const int2 *adj, int32_t n, int64_t ld, int32_t *table,
-                 const uint32_t *rows, int32_t nrows, const int32_t *terms, int32_t level1, cudaStream_t st)
+                 const uint32_t *rows, int32_t nrows, const int32_t *terms, int32_t level1, cudaStream_t st,
+                 bool u16 = false, uint32_t *vmax = nullptr)
 {
     RelaxArgs a;
     a.stamp = (int32_t *)c->stamp.ptr;
@@ -171,11 +190,14 @@ int launch_relax(emv_ctx *c, const int32_t *row_ptr, const int2 *adj, int32_t n,
     // with probability (1 - f)^d; take every vertex while that is below 10 %.
     const double deg = (double)c->relax_arcs / (double)n;
     a.dense_min = deg > 0 ? (int32_t)std::min<double>((double)n, (double)n * (1.0 - std::pow(0.1, 1.0 / deg))) : n;
-    const int vi = nrows <= 32 ? 0 : nrows <= 64 ? 1 : nrows <= 128 ? 2 : 3;
-    const void *fn = vi == 0   ? (const void *)k_relax<1>
-                     : vi == 1 ? (const void *)k_relax<2>
-                     : vi == 2 ? (const void *)k_relax<4>
-                               : (const void *)k_relax<8>;
+    a.vmax = vmax;
+    const int32_t words = u16 ? (nrows + 1) / 2 : nrows;  // int32 words a vertex record needs
+    const int vi = (words <= 32 ? 0 : words <= 64 ? 1 : words <= 128 ? 2 : 3) + (u16 ? 4 : 0);
+    static const void *const fns[8] = {(const void *)k_relax<1>,       (const void *)k_relax<2>,
+                                       (const void *)k_relax<4>,       (const void *)k_relax<8>,
+                                       (const void *)k_relax<1, true>, (const void *)k_relax<2, true>,
+                                       (const void *)k_relax<4, true>, (const void *)k_relax<8, true>};
+    const void *fn = fns[vi];
     // A warp per 8 vertices is enough; small graphs use fewer blocks (cheaper barriers).
     const int vpb = 8 * (RELAX_THREADS / 32);
     const int blocks = std::min(c->relax_blocks_max[vi], std::max(1, (n + vpb - 1) / vpb));
@@ -186,13 +208,15 @@ int launch_relax(emv_ctx *c, const int32_t *row_ptr, const int2 *adj, int32_t n,
     return EMV_OK;
 }
 
-// Rows per relaxation chunk: 128 while the chunk's 512-byte vertex records
-// fit in three quarters of L2 (the sweeps' gathers are then L2 hits and
-// larger records only add bytes per sweep), else 256, which halves the sweeps
-// of the graphs whose records stream from HBM anyway.
-int32_t relax_chunk_rows(const emv_ctx *c, int32_t n)
+// Rows per relaxation chunk: 512-byte vertex records while they fit in three
+// quarters of L2 (the sweeps' gathers are then L2 hits and larger records
+// only add bytes per sweep), else 1 KB ones, which halve the sweeps of the
+// graphs whose records stream from HBM anyway.  16-bit records hold twice
+// the rows.
+int32_t relax_chunk_rows(const emv_ctx *c, int32_t n, bool u16)
 {
-    return (int64_t)n * 512 <= c->l2_bytes * 3 / 4 ? 128 : CHUNK_ROWS;
+    const int32_t rows = (int64_t)n * 512 <= c->l2_bytes * 3 / 4 ? 128 : CHUNK_ROWS;
+    return u16 ? 2 * rows : rows;
 }
 
 int reserve_relax(emv_ctx *c, int32_t n)
@@ -504,12 +528,15 @@ int launch_merge(emv_ctx *c, int32_t *table, int64_t ld, int32_t n, int32_t k, i
     cudaError_t e = cudaSuccess;
     c->launches++;
     if (k <= MERGE_SMEM_KMAX && !c->kp->mstream_groups[(size_t)m].empty()) {
+        // the streamed merge records the level's largest value (other kernels leave it unknown)
+        CUDA_TRY(cudaMemsetAsync((uint32_t *)c->lvlmax.ptr + m, 0, sizeof(uint32_t), st));
         const int64_t b = c->kp->xs_off[(size_t)m];
         c->launches += (int64_t)c->kp->mstream_groups[(size_t)m].size() - 1;
         for (const StreamGroup &g : c->kp->mstream_groups[(size_t)m]) {
             k_merge_stream<<<(unsigned)((n + 31) / 32), 1024, (size_t)g.smem, st>>>(
                 table, ld, n, (const uint32_t *)c->kp->xs.ptr + b + g.x0, (int32_t)g.cnt,
-                (const MergePhase *)c->kp->mstream_phases.ptr + g.phase_off, (int32_t)g.nphase, d_terms, k);
+                (const MergePhase *)c->kp->mstream_phases.ptr + g.phase_off, (int32_t)g.nphase, d_terms, k,
+                (uint32_t *)c->lvlmax.ptr + m);
             e = cudaGetLastError();
             if (e != cudaSuccess) break;
         }
@@ -553,20 +580,41 @@ int run_dp(emv_ctx *c, int32_t n, const int32_t *row_ptr, const int2 *adj, int32
     c->launches++;
     CUDA_TRY(cudaEventRecord(E[ev++], st));  // 1: after fill
 
+    // Level maxima: lvlmax[m] = largest value the merge of level m wrote
+    // (level 1: its relaxation), all ones where the kernel does not record it.
+    // They reach the host one level late, so no wait idles the device.
+    uint32_t *d_max = (uint32_t *)c->lvlmax.ptr, *h_max = (uint32_t *)c->pinned + 64;
+    int64_t levels16 = 0;
+    CUDA_TRY(cudaMemsetAsync(d_max, 0xff, sizeof(uint32_t) * (EMV_MAX_K + 1), st));
+    CUDA_TRY(cudaMemsetAsync(d_max + 1, 0, sizeof(uint32_t), st));
+
     // Level 1: k single-source closures (R:1988-2031).
-    r = launch_relax(c, row_ptr, adj, n, ld, table, xs + c->kp->xs_off[1], k, d_terms, 1, st);
+    r = launch_relax(c, row_ptr, adj, n, ld, table, xs + c->kp->xs_off[1], k, d_terms, 1, st, false, d_max + 1);
     if (r) return r;
     CUDA_TRY(cudaEventRecord(E[ev++], st));  // 2: after level 1
+    CUDA_TRY(cudaMemcpyAsync(h_max + 1, d_max + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaEventRecord(c->evmax[1], st));
 
     for (int32_t m = 2; m <= k; m++) {
         const int64_t b = c->kp->xs_off[(size_t)m], cnt = c->kp->xs_off[(size_t)m + 1] - b;
         r = launch_merge(c, table, ld, n, k, m, d_terms, st);
         if (r) return r;
         CUDA_TRY(cudaEventRecord(E[ev++], st));  // merge end of level m
-        const int32_t chunk = relax_chunk_rows(c, n);
+        CUDA_TRY(cudaMemcpyAsync(h_max + m, d_max + m, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaEventRecord(c->evmax[m], st));
+        // Every merged value of level m is at most M(m-1) + M(1): the split
+        // {X \ t, t} bounds it, and relaxed values never exceed merged ones.
+        // 16-bit records when that bound is at most 32767.
+        bool u16 = false;
+        if (c->relax_bits == 0) {
+            CUDA_TRY(cudaEventSynchronize(c->evmax[m - 1]));
+            u16 = (uint64_t)h_max[m - 1] + h_max[1] <= 32767;
+        }
+        levels16 += u16;
+        const int32_t chunk = relax_chunk_rows(c, n, u16);
         for (int64_t off = 0; off < cnt; off += chunk) {
             const int32_t rows = (int32_t)std::min<int64_t>(chunk, cnt - off);
-            r = launch_relax(c, row_ptr, adj, n, ld, table, xs + b + off, rows, d_terms, 0, st);
+            r = launch_relax(c, row_ptr, adj, n, ld, table, xs + b + off, rows, d_terms, 0, st, u16);
             if (r) return r;
         }
         CUDA_TRY(cudaEventRecord(E[ev++], st));  // relax end of level m
@@ -604,6 +652,7 @@ int run_dp(emv_ctx *c, int32_t n, const int32_t *row_ptr, const int2 *adj, int32
         cudaEventElapsedTime(&ms, E[1], E[ev - 1]);
         tm->kernel_ms = ms;
         tm->relax_sweeps = (int64_t)ds.sweeps;
+        tm->relax16_levels = levels16;
     }
     return EMV_OK;
 }

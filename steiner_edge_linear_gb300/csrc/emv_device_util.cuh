@@ -99,10 +99,36 @@ template <> __device__ __forceinline__ void stcg_v<int8v>(int8v *p, int8v v)
     __stcg(q, v.a);
     __stcg(q + 1, v.b);
 }
-template <typename T> __device__ __forceinline__ T vinf();
-template <> __device__ __forceinline__ int32_t vinf<int32_t>() { return INF; }
-template <> __device__ __forceinline__ int2 vinf<int2>() { return make_int2(INF, INF); }
-template <> __device__ __forceinline__ int4 vinf<int4>() { return make_int4(INF, INF, INF, INF); }
-template <> __device__ __forceinline__ int8v vinf<int8v>() { return {vinf<int4>(), vinf<int4>()}; }
+template <typename T> __device__ __forceinline__ T vsplat(int32_t x);
+template <> __device__ __forceinline__ int32_t vsplat<int32_t>(int32_t x) { return x; }
+template <> __device__ __forceinline__ int2 vsplat<int2>(int32_t x) { return make_int2(x, x); }
+template <> __device__ __forceinline__ int4 vsplat<int4>(int32_t x) { return make_int4(x, x, x, x); }
+template <> __device__ __forceinline__ int8v vsplat<int8v>(int32_t x) { return {vsplat<int4>(x), vsplat<int4>(x)}; }
+template <typename T> __device__ __forceinline__ T vinf() { return vsplat<T>(INF); }
+
+// 16-bit records: every int32 word holds two rows.  min(a + w2, c) per
+// halfword, w2 the arc weight in both halves (the caller keeps a + w2 below
+// 2^16), and "some halfword differs".
+__device__ __forceinline__ int32_t vaddmin16(int32_t a, int32_t w2, int32_t c)
+{
+    return (int32_t)__viaddmin_u16x2((unsigned)a, (unsigned)w2, (unsigned)c);
+}
+__device__ __forceinline__ int2 vaddmin16(int2 a, int32_t w2, int2 c)
+{
+    return make_int2(vaddmin16(a.x, w2, c.x), vaddmin16(a.y, w2, c.y));
+}
+__device__ __forceinline__ int4 vaddmin16(int4 a, int32_t w2, int4 c)
+{
+    return make_int4(vaddmin16(a.x, w2, c.x), vaddmin16(a.y, w2, c.y), vaddmin16(a.z, w2, c.z),
+                     vaddmin16(a.w, w2, c.w));
+}
+__device__ __forceinline__ int8v vaddmin16(int8v a, int32_t w2, int8v c)
+{
+    return {vaddmin16(a.a, w2, c.a), vaddmin16(a.b, w2, c.b)};
+}
+__device__ __forceinline__ bool vne(int32_t a, int32_t b) { return a != b; }
+__device__ __forceinline__ bool vne(int2 a, int2 b) { return a.x != b.x || a.y != b.y; }
+__device__ __forceinline__ bool vne(int4 a, int4 b) { return a.x != b.x || a.y != b.y || a.z != b.z || a.w != b.w; }
+__device__ __forceinline__ bool vne(int8v x, int8v y) { return vne(x.a, y.a) || vne(x.b, y.b); }
 
 }  // namespace emv

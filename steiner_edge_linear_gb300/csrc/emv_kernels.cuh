@@ -40,6 +40,7 @@ struct RelaxArgs {
     int32_t max_sweeps;
     int32_t *stamp;         // n: last sweep in which the vertex changed (-1 none)
     int32_t dense_min;      // a sweep after one with more changed vertices takes every vertex
+    uint32_t *vmax;         // if set: atomicMax of every value phase C writes
 };
 
 __global__ void k_fill(int32_t *__restrict__ p, int64_t count, int32_t value)
@@ -211,7 +212,8 @@ __device__ __forceinline__ void merge_pair4(uint4 &a, const uint4 *__restrict__ 
 __global__ void __launch_bounds__(1024) k_merge_stream(int32_t *__restrict__ table, int64_t ld, int32_t n,
                                                        const uint32_t *__restrict__ xs_level, int32_t cnt,
                                                        const MergePhase *__restrict__ phases, int32_t nphase,
-                                                       const int32_t *__restrict__ terms, int32_t k)
+                                                       const int32_t *__restrict__ terms, int32_t k,
+                                                       uint32_t *__restrict__ level_max)
 {
     extern __shared__ __align__(16) uint32_t sm[];
     uint32_t *acc = sm;
@@ -219,6 +221,8 @@ __global__ void __launch_bounds__(1024) k_merge_stream(int32_t *__restrict__ tab
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int nq = nw * 4, qid = warp * 4 + (lane >> 3), ql = lane & 7;
     const int32_t v0 = blockIdx.x * 32, v = v0 + lane;
+    __shared__ uint32_t s_max;
+    if (threadIdx.x == 0) s_max = 0;
     for (int32_t i = threadIdx.x; i < cnt * 32; i += blockDim.x) acc[i] = (uint32_t)INF;
     const int parts = cnt >= nq ? 1 : nq / cnt;
     const uint4 *S4 = reinterpret_cast<const uint4 *>(S) + ql;  // staged row r, this lane's 4 vertices: S4[r * 8]
@@ -288,17 +292,23 @@ __global__ void __launch_bounds__(1024) k_merge_stream(int32_t *__restrict__ tab
         const int32_t tv = __ldg(terms + t);
         has_term |= (tv >= v0 && tv < v0 + 32);
     }
-    if (v >= n) return;
-    for (int32_t xi = warp; xi < cnt; xi += nw) {
-        const uint32_t X = __ldg(xs_level + xi);
-        uint32_t a = acc[xi * 32 + lane];
-        if (has_term)
-            for (uint32_t bits = X; bits; bits &= bits - 1) {
-                const int t = __ffs(bits) - 1;
-                if (__ldg(terms + t) == v) a = (uint32_t)table[(int64_t)(X ^ (1u << t)) * ld + v];
-            }
-        table[(int64_t)X * ld + v] = (int32_t)a;
-    }
+    uint32_t vmax = 0;  // largest value written: the relaxation's record width follows it
+    if (v < n)
+        for (int32_t xi = warp; xi < cnt; xi += nw) {
+            const uint32_t X = __ldg(xs_level + xi);
+            uint32_t a = acc[xi * 32 + lane];
+            if (has_term)
+                for (uint32_t bits = X; bits; bits &= bits - 1) {
+                    const int t = __ffs(bits) - 1;
+                    if (__ldg(terms + t) == v) a = (uint32_t)table[(int64_t)(X ^ (1u << t)) * ld + v];
+                }
+            table[(int64_t)X * ld + v] = (int32_t)a;
+            vmax = max(vmax, a);
+        }
+    vmax = __reduce_max_sync(FULL, vmax);
+    if (lane == 0) atomicMax(&s_max, vmax);
+    __syncthreads();
+    if (threadIdx.x == 0) atomicMax(level_max, s_max);
 }
 
 // Frontier sweeps over one chunk (phase B of k_relax).  A warp owns a
@@ -315,7 +325,12 @@ __global__ void __launch_bounds__(1024) k_merge_stream(int32_t *__restrict__ tab
 // one's gathers are in flight.  Only the owner writes a record and values
 // only decrease, so no atomics are needed.  Returns the number of sweeps, or
 // -1 after an error (recorded).
-template <int VEC>
+//
+// U16: 16-bit records, two rows per int32 word (64*VEC rows a record).  The
+// host takes them only when every value of the chunk's rows is at most
+// 32767; the arc weight is then clamped to 32768, so a value plus a weight
+// stays below 2^16, and a clamped sum (at least 32768) never beats a value.
+template <int VEC, bool U16>
 __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
 {
     using V = typename IVec<VEC>::T;
@@ -379,8 +394,10 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
                 for (int32_t e0 = beg;;) {
                     const unsigned sel = __ballot_sync(FULL, pull);
                     const int cnt = __popc(sel);
-                    // selected arcs compacted in this warp's slots
-                    if (pull) warcs[__popc(sel & lt)] = arc;
+                    // selected arcs compacted in this warp's slots (U16: clamped weight in both halves)
+                    if (pull)
+                        warcs[__popc(sel & lt)] =
+                            U16 ? make_int2(arc.x, (int32_t)(min((uint32_t)arc.y, 32768u) * 0x10001u)) : arc;
                     __syncwarp();
                     for (int i = 0; i < cnt; i += GROUP) {
                         V val[GROUP];
@@ -390,10 +407,11 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
                             const bool ok = i + g < cnt;
                             const int2 aw = warcs[(i + g) & 31];  // slots past cnt hold stale arcs: not used
                             wt[g] = ok ? aw.y : 0;
-                            val[g] = ok ? ldcg_v(recs + (int64_t)aw.x * 32 + lane) : vinf<V>();
+                            val[g] = ok ? ldcg_v(recs + (int64_t)aw.x * 32 + lane) : vsplat<V>(U16 ? -1 : INF);
                         }
 #pragma unroll
-                        for (int g = 0; g < GROUP; g++) acc = vmin(acc, vadd(val[g], wt[g]));
+                        for (int g = 0; g < GROUP; g++)
+                            acc = U16 ? vaddmin16(val[g], wt[g], acc) : vmin(acc, vadd(val[g], wt[g]));
                     }
                     __syncwarp();
                     e0 += 32;
@@ -419,7 +437,7 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
                         pull = pull_all || __ldcg(a.stamp + arc.x) >= s - 1;
                     }
                 }
-                const bool dec = vlt(acc, old);
+                const bool dec = U16 ? vne(acc, old) : vlt(acc, old);
                 if (dec) stcg_v(mine, acc);
                 if (__ballot_sync(FULL, dec)) {
                     any = true;
@@ -451,26 +469,35 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
 }
 
 // Phase A of a relaxation chunk: rows -> vertex-major records (vertex v owns
-// 32*VEC int32, element e = row e); in level-1 mode the rows are the k
-// single-source initialisations.  A tile is 32 vertices by all 32*VEC rows,
-// so a warp has all its 2*VEC row loads in flight before one barrier.  Also
-// resets the active flags and stamps.
-template <int VEC>
+// 32*VEC int32 words, word e = row e; U16: word e = rows e | (e + 32*VEC) << 16);
+// in level-1 mode the rows are the k single-source initialisations.  A tile
+// is 32 vertices by all 32*VEC words, so a warp has all its row loads in
+// flight before one barrier.  Rows past the chunk's are INF (U16: 0, which
+// no sweep lowers).  Also resets the active flags and stamps.
+template <int VEC, bool U16>
+__device__ __forceinline__ int32_t relax_load_value(const RelaxArgs &a, int32_t row, int32_t v)
+{
+    if (row >= a.nrows || v >= a.n) return U16 ? 0 : INF;
+    if (a.level1) return (v == __ldg(a.terms + row)) ? 0 : INF;
+    return __ldcg(a.table + (int64_t)__ldg(a.rows + row) * a.ld + v);
+}
+
+template <int VEC, bool U16>
 __device__ void relax_load_records(const RelaxArgs &a, int32_t (*tile)[33])
 {
     constexpr int R = 32 * VEC, NW = RELAX_THREADS / 32, PER = R / NW;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int32_t n = a.n, ntiles = (n + 31) >> 5, nrows = a.nrows;
+    const int32_t n = a.n, ntiles = (n + 31) >> 5;
     for (int32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int32_t v = t * 32 + lane;
         int32_t x[PER];
 #pragma unroll
         for (int q = 0; q < PER; q++) {
             const int32_t row = warp + q * NW;
-            x[q] = INF;
-            if (row < nrows && v < n) {
-                if (a.level1) x[q] = (v == __ldg(a.terms + row)) ? 0 : INF;
-                else x[q] = __ldcg(a.table + (int64_t)__ldg(a.rows + row) * a.ld + v);
+            x[q] = relax_load_value<VEC, U16>(a, row, v);
+            if (U16) {
+                const int32_t hi = relax_load_value<VEC, U16>(a, row + R, v);
+                x[q] = (int32_t)(min((uint32_t)x[q], 0xffffu) | min((uint32_t)hi, 0xffffu) << 16);
             }
         }
 #pragma unroll
@@ -491,13 +518,15 @@ __device__ void relax_load_records(const RelaxArgs &a, int32_t (*tile)[33])
     }
 }
 
-// Phase C: vertex-major records -> table rows, a whole 32-vertex tile at a time.
-template <int VEC>
+// Phase C: vertex-major records -> table rows, a whole 32-vertex tile at a
+// time; with a.vmax set, the largest value written goes to *a.vmax.
+template <int VEC, bool U16>
 __device__ void relax_store_records(const RelaxArgs &a, int32_t (*tile)[33])
 {
     constexpr int R = 32 * VEC, NW = RELAX_THREADS / 32, PER = R / NW;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int32_t n = a.n, ntiles = (n + 31) >> 5, nrows = a.nrows;
+    uint32_t vmax = 0;
     for (int32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         for (int vv = warp; vv < 32; vv += NW) {
             const int32_t v2 = t * 32 + vv;
@@ -511,9 +540,22 @@ __device__ void relax_store_records(const RelaxArgs &a, int32_t (*tile)[33])
 #pragma unroll
             for (int q = 0; q < PER; q++) {
                 const int32_t row = warp + q * NW;
-                if (row < nrows) a.table[(int64_t)__ldg(a.rows + row) * a.ld + v] = tile[row][lane];
+                const uint32_t word = (uint32_t)tile[row][lane];
+                if (U16) {
+                    const uint32_t lo = word & 0xffffu, hi = word >> 16;
+                    const int32_t xlo = lo == 0xffffu ? INF : (int32_t)lo, xhi = hi == 0xffffu ? INF : (int32_t)hi;
+                    if (row < nrows) a.table[(int64_t)__ldg(a.rows + row) * a.ld + v] = xlo;
+                    if (row + R < nrows) a.table[(int64_t)__ldg(a.rows + row + R) * a.ld + v] = xhi;
+                } else if (row < nrows) {
+                    a.table[(int64_t)__ldg(a.rows + row) * a.ld + v] = (int32_t)word;
+                    vmax = max(vmax, word);
+                }
             }
         __syncthreads();
+    }
+    if (a.vmax) {
+        vmax = __reduce_max_sync(FULL, vmax);
+        if (lane == 0) atomicMax(a.vmax, vmax);
     }
 }
 
@@ -524,20 +566,20 @@ __device__ void relax_store_records(const RelaxArgs &a, int32_t (*tile)[33])
 // bound), ending after a sweep that changes nothing; C. records -> rows.
 // Records and stamps are read with ld.global.cg (L2), never through a stale
 // L1 line.
-template <int VEC>
+template <int VEC, bool U16 = false>
 __global__ void __launch_bounds__(RELAX_THREADS, 2) k_relax(RelaxArgs a)
 {
-    __shared__ int32_t tile[32 * VEC][33];  // 32 vertices by all rows of the chunk
+    __shared__ int32_t tile[32 * VEC][33];  // 32 vertices by all words of the chunk's records
     __shared__ int s_ok;
-    relax_load_records<VEC>(a, tile);
+    relax_load_records<VEC, U16>(a, tile);
     if (!grid_barrier(a.ctrl, &s_ok)) {
         if (threadIdx.x == 0) atomicOr(&a.stat->err, a.ctrl[C_ERR]);
         return;
     }
-    const int32_t s = relax_sweeps<VEC>(a, &s_ok);
+    const int32_t s = relax_sweeps<VEC, U16>(a, &s_ok);
     if (s < 0) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.stat->sweeps, (unsigned long long)s);
-    relax_store_records<VEC>(a, tile);
+    relax_store_records<VEC, U16>(a, tile);
 }
 
 // ------------------------------------------------------------- traceback

@@ -51,11 +51,14 @@ struct KPlan {
 struct emv_ctx {
     int device = 0;
     int sms = 0;
-    int relax_blocks_max[4] = {0, 0, 0, 0};  // cooperative grid of k_relax<1>, <2>, <4>, <8>
+    int relax_blocks_max[8] = {};  // cooperative grid of k_relax<1>, <2>, <4>, <8>, then the 16-bit ones
     int64_t l2_bytes = 0;
     int64_t sweep_limit = 0;       // relaxation sweeps per chunk, 0 = n + 1
+    int32_t relax_bits = 0;        // 0: 16-bit records where bounded, 32: always 32-bit
     int64_t relax_arcs = 0;       // arcs of the graph being relaxed (dense-sweep threshold)
     DevBuf ctrl, stat;             // relaxation barrier words, solve status
+    DevBuf lvlmax;                 // per level: largest value its merge (level 1: relaxation) wrote
+    cudaEvent_t evmax[EMV_MAX_K + 1] = {};  // level m's maximum has reached the pinned buffer
     DevBuf scratch, act;           // vertex-major chunk buffer, active flags
     DevBuf stamp;                  // per vertex: last sweep in which it changed
     DevBuf adj;                    // packed (col, w) arcs
@@ -85,4 +88,4 @@ struct emv_ctx {
 void subset_levels(int32_t k, std::vector<uint32_t> &xs, std::vector<int64_t> &off);
 int prepare_subsets(emv_ctx *c, int32_t k, cudaStream_t st);
 int reserve_relax(emv_ctx *c, int32_t n);
-int32_t relax_chunk_rows(const emv_ctx *c, int32_t n);
+int32_t relax_chunk_rows(const emv_ctx *c, int32_t n, bool u16);

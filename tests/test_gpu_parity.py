@@ -134,6 +134,71 @@ def test_large_k_whole_table(emv, orc, solver, n, degree, k):
     check_tree(csr.n, inst.edges, res.tree, csr.terminals, res.cost)
 
 
+def _u16_levels(table, terms):
+    """Levels m >= 2 the solver relaxes with 16-bit records: those with
+    M(m-1) + M(1) <= 32767, M(j) the largest value level j's merge writes
+    (recomputed here from the oracle's lower levels, terminal override
+    included) and M(1) the largest single-source distance."""
+    k = len(terms)
+    M = {1: int(max(table[1 << i].max() for i in range(k)))}
+    for m in range(2, k):
+        mx = 0
+        for X in range(1, 1 << k):
+            if bin(X).count("1") != m:
+                continue
+            best = None
+            Y = (X - 1) & X
+            while Y:
+                if Y < (X ^ Y):
+                    s = table[Y].astype(np.int64) + table[X ^ Y]
+                    best = s if best is None else np.minimum(best, s)
+                Y = (Y - 1) & X
+            for t in range(k):
+                if X >> t & 1:
+                    best[terms[t]] = table[X ^ (1 << t)][terms[t]]
+            mx = max(mx, int(best.max()))
+        M[m] = mx
+    return sum(1 for m in range(2, k + 1) if M[m - 1] + M[1] <= 32767)
+
+
+@pytest.mark.parametrize("ew,kind", [(100, "all"), (3000, "some"), (8000, "none")])
+def test_relax_record_widths_match_oracle(emv, orc, ew, kind):
+    """16-bit relaxation records are taken per level while its values are
+    provably at most 32767: weights up to 100 keep every level 16-bit, 3000
+    the lower levels only, 8000 none.  The level count equals the rule's,
+    and the table equals the oracle's with automatic and with 32-bit records."""
+    k = 10
+    inst = emv.StpInstance.regular(6000, 6, 1, ew, k, 515)
+    csr = emv.Csr.from_stp(inst)
+    want, want_cost = orc.emv_table(csr.n, csr.row_ptr, csr.col, csr.w, csr.terminals, threads=8)
+    expect = _u16_levels(want, list(csr.terminals))
+    assert {"all": expect == k - 1, "some": 0 < expect < k - 1, "none": expect == 0}[kind]
+    with emv.Solver(0) as s:
+        for bits in (0, 32):
+            s.set_relax_records(bits)
+            res = s.solve(csr, tree=True, table=True)
+            assert res.timing["relax16_levels"] == (expect if bits == 0 else 0)
+            assert res.cost == want_cost
+            mism = np.argwhere(res.table != want)
+            assert mism.size == 0, f"bits {bits}: {len(mism)} cells differ, first (X, v) = {mism[:5].tolist()}"
+            check_tree(csr.n, inst.edges, res.tree, csr.terminals, res.cost)
+        with pytest.raises(emv.EmvError):
+            s.set_relax_records(16)
+
+
+def test_relax_512_row_chunks_equal_32_bit_records(emv):
+    """Records past three quarters of L2 (n = 2^18) take 1 KB per vertex: 512
+    rows of 16 bits against 256 of 32; both tables are identical."""
+    inst = emv.StpInstance.regular(1 << 18, 6, 1, 100, 11, 2718)
+    csr = emv.Csr.from_stp(inst)
+    with emv.Solver(0) as s:
+        a = s.solve(csr, table=True)
+        s.set_relax_records(32)
+        b = s.solve(csr, table=True)
+    assert a.timing["relax16_levels"] == 10 and b.timing["relax16_levels"] == 0
+    assert a.cost == b.cost and np.array_equal(a.table, b.table)
+
+
 def test_bad_inputs_report_status(emv, solver):
     disc = emv.StpInstance.from_text(
         "section graph\nnodes 4\nedges 2\ne 1 2 3\ne 3 4 5\nend\nsection terminals\nterminals 2\nt 1\nt 3\nend\n")
