@@ -172,12 +172,14 @@ int emv_destroy(emv_ctx *ctx);
  * usable: a latency bound for callers that prefer an error to an unusually
  * long solve.  No reference counterpart (its Dijkstra has no budget). */
 int emv_set_sweep_limit(emv_ctx *ctx, int64_t limit);
-/* Relaxation record width of the context's later solves: 0 (the default)
- * takes 16-bit records for every level whose values are provably at most
- * 32767 (twice the rows per chunk at the same bytes), 32 always takes 32-bit
- * ones.  Results are identical either way.  No reference counterpart (its
- * Dijkstra works on the int32 table directly). */
-int emv_set_relax_records(emv_ctx *ctx, int32_t bits);
+/* Width of the DP values inside the kernels of the context's later solves:
+ * 0 (the default) stages a level's merge rows as 16-bit values when every
+ * sum of two of them is provably at most 65533, and relaxes a level with
+ * 16-bit records when its values are provably at most 32767 (twice the rows
+ * per chunk at the same bytes); 32 always keeps 32 bits.  The table is int32
+ * and identical either way.  No reference counterpart (it works on the int32
+ * table directly). */
+int emv_set_value_bits(emv_ctx *ctx, int32_t bits);
 
 /* Per-phase device times of the last solve (CUDA events, ms). */
 typedef struct emv_timing {
@@ -190,6 +192,7 @@ typedef struct emv_timing {
     int64_t relax_sweeps; /* frontier sweeps summed over chunks          */
     int64_t launches;     /* kernel launches issued by the solve         */
     int64_t relax16_levels; /* levels relaxed with 16-bit records        */
+    int64_t merge16_levels; /* levels merged from 16-bit staged rows     */
 } emv_timing;
 
 /* Mirrors emv_kernel(n, m, k, c, C, q, kk, f_v, pos, adj, ...) (R:1966-2139)

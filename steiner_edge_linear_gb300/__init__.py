@@ -64,7 +64,8 @@ class _Graph(ctypes.Structure):
 class _Timing(ctypes.Structure):
     _fields_ = [("zero_ms", ctypes.c_float), ("level1_ms", ctypes.c_float), ("merge_ms", ctypes.c_float),
                 ("relax_ms", ctypes.c_float), ("traceback_ms", ctypes.c_float), ("kernel_ms", ctypes.c_float),
-                ("relax_sweeps", ctypes.c_int64), ("launches", ctypes.c_int64), ("relax16_levels", ctypes.c_int64)]
+                ("relax_sweeps", ctypes.c_int64), ("launches", ctypes.c_int64), ("relax16_levels", ctypes.c_int64),
+                ("merge16_levels", ctypes.c_int64)]
 
 
 class _Result(ctypes.Structure):
@@ -126,7 +127,7 @@ SIGNATURES = {
     "emv_create": (ctypes.c_int, [ctypes.POINTER(_P), _I32]),
     "emv_destroy": (ctypes.c_int, [_P]),
     "emv_set_sweep_limit": (ctypes.c_int, [_P, _I64]),
-    "emv_set_relax_records": (ctypes.c_int, [_P, ctypes.c_int32]),
+    "emv_set_value_bits": (ctypes.c_int, [_P, ctypes.c_int32]),
     "emv_kernel_dev": (ctypes.c_int, [_P, _I32, _I64, _P, _P, _P, _I32, _P, _P, _I64, ctypes.POINTER(_I64), _P]),
     "emv_solve": (ctypes.c_int, [_P, ctypes.POINTER(_Graph), _P, _I32, _I32, ctypes.POINTER(_Result), _P]),
     "emv_solve_dev": (ctypes.c_int, [_P, ctypes.POINTER(_Graph), _P, _I32, _I32, ctypes.POINTER(_Result), _P]),
@@ -460,9 +461,10 @@ class Solver:
         solve that hits the cap raises EmvError with EMV_ERR_TIMEOUT."""
         _check(self._lib.emv_set_sweep_limit(self._ctx, int(limit)))
 
-    def set_relax_records(self, bits: int) -> None:
-        """Relaxation record width: 0 = 16-bit where the level's values allow, 32 = always 32-bit."""
-        _check(self._lib.emv_set_relax_records(self._ctx, int(bits)))
+    def set_value_bits(self, bits: int) -> None:
+        """Width of the values in the merge's staged rows and the relaxation's
+        records: 0 = 16 bits where the level maxima allow, 32 = always 32."""
+        _check(self._lib.emv_set_value_bits(self._ctx, int(bits)))
 
     def kernel_dev(self, n: int, arcs: int, row_ptr: int, col: int, w: int, terminals: Sequence[int],
                    table: int, ld: int, stream: Optional[int] = None) -> int:

@@ -122,10 +122,10 @@ extern "C" int emv_set_sweep_limit(emv_ctx *c, int64_t limit)
     return EMV_OK;
 }
 
-extern "C" int emv_set_relax_records(emv_ctx *c, int32_t bits)
+extern "C" int emv_set_value_bits(emv_ctx *c, int32_t bits)
 {
-    if (!c || (bits != 0 && bits != 32)) return emv_fail(EMV_ERR_BAD_INPUT, "emv_set_relax_records: bits 0 or 32");
-    c->relax_bits = bits;
+    if (!c || (bits != 0 && bits != 32)) return emv_fail(EMV_ERR_BAD_INPUT, "emv_set_value_bits: bits 0 or 32");
+    c->value_bits = bits;
     return EMV_OK;
 }
 
@@ -233,6 +233,11 @@ constexpr int32_t MERGE_SMEM_KMAX = 15;  // staged slots must fit 16 bits
 
 constexpr int32_t STREAM_SMEM_BYTES = 224 * 1024;
 
+// Accumulator space of a streamed-merge group of g subsets, in 128-byte rows:
+// one per subset, two where the 16-bit kernel keeps one uint32 per vertex
+// (g <= 64: its 128 quarter-warps then split each subset's pairs).
+static int64_t stream_acc_rows(int64_t g) { return g <= 64 ? 2 * g : g; }
+
 // Plan of the streamed merge (k_merge_stream) for every level of k.  The
 // subsets of level m are cut into groups whose accumulators (128 bytes per
 // subset and 32 vertices) leave room for staged rows; for each group and each
@@ -260,7 +265,7 @@ bool plan_level(const std::vector<uint32_t> &xs, const std::vector<int64_t> &off
                 std::vector<HostGroup> &groups, int64_t &cost)
 {
     const int64_t lvl = off[(size_t)m], cnt = off[(size_t)m + 1] - lvl;
-    const int64_t cap = smem_bytes / 128 - gx - 1;  // staged rows besides the INF pad row
+    const int64_t cap = smem_bytes / 128 - stream_acc_rows(gx) - 1;  // staged rows besides the INF pad row
     if (cap < 2) return false;
     data.clear();
     groups.clear();
@@ -332,7 +337,7 @@ bool plan_level(const std::vector<uint32_t> &xs, const std::vector<int64_t> &off
             }
             emit();
         }
-        G.smem = (g + max_rows + 1) * 128;
+        G.smem = (stream_acc_rows(g) + max_rows + 1) * 128;
         cost += 64;
         groups.push_back(std::move(G));
     }
@@ -512,7 +517,7 @@ static cudaError_t merge_smem_launch(emv_ctx *c, int32_t *table, int64_t ld, int
 // Merge of level m: the shared-memory kernel with the widest vertex block
 // whose staging fits, else the direct kernel (k above MERGE_SMEM_KMAX).
 int launch_merge(emv_ctx *c, int32_t *table, int64_t ld, int32_t n, int32_t k, int32_t m, const int32_t *d_terms,
-                 cudaStream_t st)
+                 cudaStream_t st, bool u16 = false)
 {
     if (!c->merge_attr) {
         const void *fns[6] = {(const void *)k_merge_smem<32>, (const void *)k_merge_smem<16>,
@@ -522,21 +527,31 @@ int launch_merge(emv_ctx *c, int32_t *table, int64_t ld, int32_t n, int32_t k, i
             CUDA_TRY(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, MERGE_SMEM_BYTES));
         CUDA_TRY(cudaFuncSetAttribute((const void *)k_merge_stream, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       STREAM_SMEM_BYTES));
+        CUDA_TRY(cudaFuncSetAttribute((const void *)k_merge_stream16, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      STREAM_SMEM_BYTES));
         c->merge_attr = true;
     }
     const int64_t nstage = c->kp->xs_off[(size_t)m];
     cudaError_t e = cudaSuccess;
+    c->merge16_last = false;
     c->launches++;
     if (k <= MERGE_SMEM_KMAX && !c->kp->mstream_groups[(size_t)m].empty()) {
         // the streamed merge records the level's largest value (other kernels leave it unknown)
         CUDA_TRY(cudaMemsetAsync((uint32_t *)c->lvlmax.ptr + m, 0, sizeof(uint32_t), st));
         const int64_t b = c->kp->xs_off[(size_t)m];
         c->launches += (int64_t)c->kp->mstream_groups[(size_t)m].size() - 1;
+        // 16-bit staging reads int2 pairs of vertices: even stride and base
+        u16 = u16 && ld % 2 == 0 && ((uintptr_t)table & 7) == 0;
+        c->merge16_last = u16;
         for (const StreamGroup &g : c->kp->mstream_groups[(size_t)m]) {
-            k_merge_stream<<<(unsigned)((n + 31) / 32), 1024, (size_t)g.smem, st>>>(
-                table, ld, n, (const uint32_t *)c->kp->xs.ptr + b + g.x0, (int32_t)g.cnt,
-                (const MergePhase *)c->kp->mstream_phases.ptr + g.phase_off, (int32_t)g.nphase, d_terms, k,
-                (uint32_t *)c->lvlmax.ptr + m);
+            const uint32_t *xg = (const uint32_t *)c->kp->xs.ptr + b + g.x0;
+            const MergePhase *pg = (const MergePhase *)c->kp->mstream_phases.ptr + g.phase_off;
+            if (u16)
+                k_merge_stream16<<<(unsigned)((n + 63) / 64), 1024, (size_t)g.smem, st>>>(
+                    table, ld, n, xg, (int32_t)g.cnt, pg, (int32_t)g.nphase, d_terms, k, (uint32_t *)c->lvlmax.ptr + m);
+            else
+                k_merge_stream<<<(unsigned)((n + 31) / 32), 1024, (size_t)g.smem, st>>>(
+                    table, ld, n, xg, (int32_t)g.cnt, pg, (int32_t)g.nphase, d_terms, k, (uint32_t *)c->lvlmax.ptr + m);
             e = cudaGetLastError();
             if (e != cudaSuccess) break;
         }
@@ -584,7 +599,7 @@ int run_dp(emv_ctx *c, int32_t n, const int32_t *row_ptr, const int2 *adj, int32
     // (level 1: its relaxation), all ones where the kernel does not record it.
     // They reach the host one level late, so no wait idles the device.
     uint32_t *d_max = (uint32_t *)c->lvlmax.ptr, *h_max = (uint32_t *)c->pinned + 64;
-    int64_t levels16 = 0;
+    int64_t levels16 = 0, merges16 = 0;
     CUDA_TRY(cudaMemsetAsync(d_max, 0xff, sizeof(uint32_t) * (EMV_MAX_K + 1), st));
     CUDA_TRY(cudaMemsetAsync(d_max + 1, 0, sizeof(uint32_t), st));
 
@@ -597,8 +612,19 @@ int run_dp(emv_ctx *c, int32_t n, const int32_t *row_ptr, const int2 *adj, int32
 
     for (int32_t m = 2; m <= k; m++) {
         const int64_t b = c->kp->xs_off[(size_t)m], cnt = c->kp->xs_off[(size_t)m + 1] - b;
-        r = launch_merge(c, table, ld, n, k, m, d_terms, st);
+        // 16-bit merge staging when every sum of two lower-level values is
+        // at most 65533 (M(j) bounds level j's values); from level 3 on, where
+        // waiting for level m-1's maximum leaves its relaxation queued.
+        bool m16 = false;
+        if (c->value_bits == 0 && m >= 3) {
+            CUDA_TRY(cudaEventSynchronize(c->evmax[m - 1]));
+            uint64_t worst = 0;
+            for (int32_t j = 1; 2 * j <= m; j++) worst = std::max<uint64_t>(worst, (uint64_t)h_max[j] + h_max[m - j]);
+            m16 = worst <= 65533;
+        }
+        r = launch_merge(c, table, ld, n, k, m, d_terms, st, m16);
         if (r) return r;
+        merges16 += c->merge16_last;
         CUDA_TRY(cudaEventRecord(E[ev++], st));  // merge end of level m
         CUDA_TRY(cudaMemcpyAsync(h_max + m, d_max + m, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaEventRecord(c->evmax[m], st));
@@ -606,7 +632,7 @@ int run_dp(emv_ctx *c, int32_t n, const int32_t *row_ptr, const int2 *adj, int32
         // {X \ t, t} bounds it, and relaxed values never exceed merged ones.
         // 16-bit records when that bound is at most 32767.
         bool u16 = false;
-        if (c->relax_bits == 0) {
+        if (c->value_bits == 0) {
             CUDA_TRY(cudaEventSynchronize(c->evmax[m - 1]));
             u16 = (uint64_t)h_max[m - 1] + h_max[1] <= 32767;
         }
@@ -653,6 +679,7 @@ int run_dp(emv_ctx *c, int32_t n, const int32_t *row_ptr, const int2 *adj, int32
         tm->kernel_ms = ms;
         tm->relax_sweeps = (int64_t)ds.sweeps;
         tm->relax16_levels = levels16;
+        tm->merge16_levels = merges16;
     }
     return EMV_OK;
 }

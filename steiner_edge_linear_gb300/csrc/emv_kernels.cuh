@@ -311,6 +311,156 @@ __global__ void __launch_bounds__(1024) k_merge_stream(int32_t *__restrict__ tab
     if (threadIdx.x == 0) atomicMax(level_max, s_max);
 }
 
+// 16-bit streamed merge: the same plan and phases as k_merge_stream, for a
+// level whose sums of two staged values are all at most 65533 (the host
+// checks the level maxima).  A block takes 64 vertices; a staged row holds
+// them as 32 words of two 16-bit values (the same 128 bytes per row), so one
+// 16-byte shared load brings 8 vertices and one min(y + z, a) per halfword
+// (__viaddmin_u16x2) serves two.  The pad row is all ones: a pad pair sums to
+// at least 0xfffe, above every real candidate.  Rows are staged through
+// registers (int2 loads, packed to 16 bits), so the table stride and base
+// must be even.  Minima live in acc as 16-bit pairs, or as one uint32 per
+// vertex where quarters split a subset's pairs (shared-memory atomicMin).
+__device__ __forceinline__ void merge_pair8(uint4 &a, const uint4 *__restrict__ S4, uint32_t pr)
+{
+    const uint4 y = S4[(pr & 0xffffu) * 8];
+    const uint4 z = S4[(pr >> 16) * 8];
+    a.x = __viaddmin_u16x2(y.x, z.x, a.x);
+    a.y = __viaddmin_u16x2(y.y, z.y, a.y);
+    a.z = __viaddmin_u16x2(y.z, z.z, a.z);
+    a.w = __viaddmin_u16x2(y.w, z.w, a.w);
+}
+
+__device__ __forceinline__ uint32_t pack16(int2 x)
+{
+    return min((uint32_t)x.x, 0xffffu) | min((uint32_t)x.y, 0xffffu) << 16;
+}
+
+__global__ void __launch_bounds__(1024) k_merge_stream16(int32_t *__restrict__ table, int64_t ld, int32_t n,
+                                                         const uint32_t *__restrict__ xs_level, int32_t cnt,
+                                                         const MergePhase *__restrict__ phases, int32_t nphase,
+                                                         const int32_t *__restrict__ terms, int32_t k,
+                                                         uint32_t *__restrict__ level_max)
+{
+    extern __shared__ __align__(16) uint32_t sm[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int nq = nw * 4, qid = warp * 4 + (lane >> 3), ql = lane & 7;
+    const int parts = cnt >= nq ? 1 : nq / cnt;
+    const int acc_words = parts > 1 ? 64 : 32;  // per subset
+    uint32_t *acc = sm;
+    uint32_t *S = sm + (size_t)cnt * acc_words;
+    const int32_t v0 = blockIdx.x * 64, va = v0 + 2 * lane;  // this lane's vertices in staging and epilogue
+    const bool full = v0 + 64 <= n;
+    __shared__ uint32_t s_max;
+    if (threadIdx.x == 0) s_max = 0;
+    for (int32_t i = threadIdx.x; i < cnt * acc_words; i += blockDim.x) acc[i] = 0xffffffffu;
+    const uint4 *S4 = reinterpret_cast<const uint4 *>(S) + ql;  // staged row r, this lane's 8 vertices: S4[r * 8]
+    const uint4 ones4 = make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
+    for (int32_t ph = 0; ph < nphase; ph++) {
+        const MergePhase P = phases[ph];
+        __syncthreads();
+        // staging: a warp takes 32 rows at a time, 8 row loads in flight per lane
+        for (int32_t c0 = warp * 32; c0 < P.nrows; c0 += nw * 32) {
+            const uint32_t myr = c0 + lane < P.nrows ? __ldg(P.rows + c0 + lane) : 0u;
+            const int32_t nr = min(32, P.nrows - c0);
+            for (int32_t j0 = 0; j0 < nr; j0 += 8) {
+                int2 x[8];
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    const uint32_t r = __shfl_sync(FULL, myr, j0 + u);
+                    const int32_t *row = table + (int64_t)r * ld;
+                    x[u] = make_int2(-1, -1);
+                    if (j0 + u < nr) {
+                        if (full) x[u] = __ldg(reinterpret_cast<const int2 *>(row + v0) + lane);
+                        else if (va < n) x[u] = make_int2(__ldg(row + va), va + 1 < n ? __ldg(row + va + 1) : -1);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 8; u++)
+                    if (j0 + u < nr) S[(c0 + j0 + u) * 32 + lane] = pack16(x[u]);
+            }
+        }
+        if (warp == nw - 1) S[P.nrows * 32 + lane] = 0xffffffffu;
+        __syncthreads();
+        for (int32_t t = qid; t < cnt * parts; t += nq) {
+            const int32_t xi = t / parts, part = t - xi * parts;
+            const uint32_t qb = __ldg(P.qoff + xi);
+            const int32_t quads = (int32_t)(__ldg(P.qoff + xi + 1) - qb);
+            const uint4 *Q = reinterpret_cast<const uint4 *>(P.pairs) + qb;
+            uint4 a0 = ones4, a1 = ones4;
+            int32_t qi = part;
+            const uint4 zq = make_uint4(0, 0, 0, 0);
+            uint4 q = qi < quads ? __ldg(Q + qi) : zq;
+            uint4 q1 = qi + parts < quads ? __ldg(Q + qi + parts) : zq;
+            while (qi < quads) {
+                const int32_t q2i = qi + 2 * parts;
+                const uint4 q2 = q2i < quads ? __ldg(Q + q2i) : zq;
+                merge_pair8(a0, S4, q.x);
+                merge_pair8(a1, S4, q.y);
+                merge_pair8(a0, S4, q.z);
+                merge_pair8(a1, S4, q.w);
+                q = q1;
+                q1 = q2;
+                qi += parts;
+            }
+            const uint4 r = make_uint4(__vminu2(a0.x, a1.x), __vminu2(a0.y, a1.y), __vminu2(a0.z, a1.z),
+                                       __vminu2(a0.w, a1.w));
+            if (parts == 1) {
+                uint4 *A4 = reinterpret_cast<uint4 *>(acc + xi * 32 + ql * 4);
+                const uint4 o = *A4;
+                *A4 = make_uint4(__vminu2(o.x, r.x), __vminu2(o.y, r.y), __vminu2(o.z, r.z), __vminu2(o.w, r.w));
+            } else {
+                uint32_t *A = acc + xi * 64 + ql * 8;
+                const uint32_t w[4] = {r.x, r.y, r.z, r.w};
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    atomicMin(A + 2 * i, w[i] & 0xffffu);
+                    atomicMin(A + 2 * i + 1, w[i] >> 16);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    bool has_term = false;
+    for (int t = 0; t < k; t++) {
+        const int32_t tv = __ldg(terms + t);
+        has_term |= (tv >= v0 && tv < v0 + 64);
+    }
+    uint32_t vmax = 0;  // largest value written: the relaxation's record width follows it
+    if (va < n)
+        for (int32_t xi = warp; xi < cnt; xi += nw) {
+            const uint32_t X = __ldg(xs_level + xi);
+            uint32_t a0, a1;
+            if (parts > 1) {
+                a0 = acc[xi * 64 + 2 * lane];
+                a1 = acc[xi * 64 + 2 * lane + 1];
+            } else {
+                const uint32_t wd = acc[xi * 32 + lane];
+                a0 = wd & 0xffffu;
+                a1 = wd >> 16;
+            }
+            if (has_term)
+                for (uint32_t bits = X; bits; bits &= bits - 1) {
+                    const int t = __ffs(bits) - 1;
+                    const int32_t tv = __ldg(terms + t);
+                    if (tv == va) a0 = (uint32_t)table[(int64_t)(X ^ (1u << t)) * ld + va];
+                    if (tv == va + 1) a1 = (uint32_t)table[(int64_t)(X ^ (1u << t)) * ld + va + 1];
+                }
+            int32_t *dst = table + (int64_t)X * ld + va;
+            if (va + 1 < n) {
+                *reinterpret_cast<int2 *>(dst) = make_int2((int32_t)a0, (int32_t)a1);
+                vmax = max(vmax, max(a0, a1));
+            } else {
+                *dst = (int32_t)a0;
+                vmax = max(vmax, a0);
+            }
+        }
+    vmax = __reduce_max_sync(FULL, vmax);
+    if (lane == 0) atomicMax(&s_max, vmax);
+    __syncthreads();
+    if (threadIdx.x == 0) atomicMax(level_max, s_max);
+}
+
 // Frontier sweeps over one chunk (phase B of k_relax).  A warp owns a
 // contiguous range of n / W vertices (W warps in the grid, so the shares
 // differ by one vertex at most) and takes them TASK_V at a time: it

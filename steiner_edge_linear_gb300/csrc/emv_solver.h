@@ -54,7 +54,8 @@ struct emv_ctx {
     int relax_blocks_max[8] = {};  // cooperative grid of k_relax<1>, <2>, <4>, <8>, then the 16-bit ones
     int64_t l2_bytes = 0;
     int64_t sweep_limit = 0;       // relaxation sweeps per chunk, 0 = n + 1
-    int32_t relax_bits = 0;        // 0: 16-bit records where bounded, 32: always 32-bit
+    int32_t value_bits = 0;        // 0: 16-bit merge staging / relaxation records where bounded, 32: never
+    bool merge16_last = false;     // the last launch_merge took the 16-bit kernel
     int64_t relax_arcs = 0;       // arcs of the graph being relaxed (dense-sweep threshold)
     DevBuf ctrl, stat;             // relaxation barrier words, solve status
     DevBuf lvlmax;                 // per level: largest value its merge (level 1: relaxation) wrote

@@ -134,11 +134,13 @@ def test_large_k_whole_table(emv, orc, solver, n, degree, k):
     check_tree(csr.n, inst.edges, res.tree, csr.terminals, res.cost)
 
 
-def _u16_levels(table, terms):
-    """Levels m >= 2 the solver relaxes with 16-bit records: those with
-    M(m-1) + M(1) <= 32767, M(j) the largest value level j's merge writes
-    (recomputed here from the oracle's lower levels, terminal override
-    included) and M(1) the largest single-source distance."""
+def _narrow_levels(table, terms):
+    """Levels the solver takes with 16-bit values, recomputed from the
+    oracle's table: M(j) is the largest value level j's merge writes (from the
+    lower levels, terminal override included), M(1) the largest single-source
+    distance.  Level m >= 2 relaxes with 16-bit records when M(m-1) + M(1) <=
+    32767; level m >= 3 merges from 16-bit rows when every M(j) + M(m-j) <=
+    65533.  Returns (relaxed, merged) level counts."""
     k = len(terms)
     M = {1: int(max(table[1 << i].max() for i in range(k)))}
     for m in range(2, k):
@@ -158,44 +160,54 @@ def _u16_levels(table, terms):
                     best[terms[t]] = table[X ^ (1 << t)][terms[t]]
             mx = max(mx, int(best.max()))
         M[m] = mx
-    return sum(1 for m in range(2, k + 1) if M[m - 1] + M[1] <= 32767)
+    relaxed = sum(1 for m in range(2, k + 1) if M[m - 1] + M[1] <= 32767)
+    merged = sum(1 for m in range(3, k + 1) if max(M[j] + M[m - j] for j in range(1, m // 2 + 1)) <= 65533)
+    return relaxed, merged
 
 
-@pytest.mark.parametrize("ew,kind", [(100, "all"), (3000, "some"), (8000, "none")])
-def test_relax_record_widths_match_oracle(emv, orc, ew, kind):
-    """16-bit relaxation records are taken per level while its values are
-    provably at most 32767: weights up to 100 keep every level 16-bit, 3000
-    the lower levels only, 8000 none.  The level count equals the rule's,
-    and the table equals the oracle's with automatic and with 32-bit records."""
+# weight range -> which levels take 16-bit relaxation records and merge rows
+WIDTH_CASES = {100: ("all", "all"), 3000: ("some", "all"), 5000: ("some", "some"), 8000: ("none", "none")}
+
+
+@pytest.mark.parametrize("ew", sorted(WIDTH_CASES))
+def test_value_widths_match_oracle(emv, orc, ew):
+    """16-bit values are taken per level only where the level maxima bound
+    them: weights up to 100 keep every level 16-bit, larger weights the lower
+    levels only or none.  The level counts equal the rule's, and the table
+    equals the oracle's with automatic and with 32-bit values."""
     k = 10
     inst = emv.StpInstance.regular(6000, 6, 1, ew, k, 515)
     csr = emv.Csr.from_stp(inst)
     want, want_cost = orc.emv_table(csr.n, csr.row_ptr, csr.col, csr.w, csr.terminals, threads=8)
-    expect = _u16_levels(want, list(csr.terminals))
-    assert {"all": expect == k - 1, "some": 0 < expect < k - 1, "none": expect == 0}[kind]
+    relaxed, merged = _narrow_levels(want, list(csr.terminals))
+    kinds = tuple("all" if c == top else "none" if c == 0 else "some" for c, top in ((relaxed, k - 1), (merged, k - 2)))
+    assert kinds == WIDTH_CASES[ew]
     with emv.Solver(0) as s:
         for bits in (0, 32):
-            s.set_relax_records(bits)
+            s.set_value_bits(bits)
             res = s.solve(csr, tree=True, table=True)
-            assert res.timing["relax16_levels"] == (expect if bits == 0 else 0)
+            assert res.timing["relax16_levels"] == (relaxed if bits == 0 else 0)
+            assert res.timing["merge16_levels"] == (merged if bits == 0 else 0)
             assert res.cost == want_cost
             mism = np.argwhere(res.table != want)
             assert mism.size == 0, f"bits {bits}: {len(mism)} cells differ, first (X, v) = {mism[:5].tolist()}"
             check_tree(csr.n, inst.edges, res.tree, csr.terminals, res.cost)
         with pytest.raises(emv.EmvError):
-            s.set_relax_records(16)
+            s.set_value_bits(16)
 
 
-def test_relax_512_row_chunks_equal_32_bit_records(emv):
-    """Records past three quarters of L2 (n = 2^18) take 1 KB per vertex: 512
-    rows of 16 bits against 256 of 32; both tables are identical."""
-    inst = emv.StpInstance.regular(1 << 18, 6, 1, 100, 11, 2718)
+def test_wide_records_and_partial_merge_block_equal_32_bit_values(emv):
+    """Records past three quarters of L2 (n = 2^18 + 40) take 1 KB per vertex:
+    512 rows of 16 bits against 256 of 32; the last 64-vertex merge block is
+    partial.  Both tables are identical."""
+    inst = emv.StpInstance.regular((1 << 18) + 40, 6, 1, 100, 11, 2718)
     csr = emv.Csr.from_stp(inst)
     with emv.Solver(0) as s:
         a = s.solve(csr, table=True)
-        s.set_relax_records(32)
+        s.set_value_bits(32)
         b = s.solve(csr, table=True)
-    assert a.timing["relax16_levels"] == 10 and b.timing["relax16_levels"] == 0
+    assert a.timing["relax16_levels"] == 10 and a.timing["merge16_levels"] == 9
+    assert b.timing["relax16_levels"] == 0 and b.timing["merge16_levels"] == 0
     assert a.cost == b.cost and np.array_equal(a.table, b.table)
 
 
