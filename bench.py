@@ -275,18 +275,14 @@ def run_single(args, dist: Dist, cfg: dict = SINGLE, cfg_name: str = SINGLE_NAME
     kernel_ms = statistics.median(t["kernel_ms"] for t in timings)
     launches = int(statistics.median(t["launches"] for t in timings))
     rows = (1 << k) - 1
-    from math import comb
-    # chunk rule of the library (relax_chunk_rows): 128 rows while 512-byte records fit 3/4 of L2, else 256
-    l2 = getattr(torch.cuda.get_device_properties(0), "L2_cache_size", 126 << 20)
-    chunk = 128 if n * 512 <= l2 * 3 // 4 else 256
-    relax_launches = 1 + sum(-(-comb(k, mm) // chunk) for mm in range(2, k + 1))
+    relax_launches = int(statistics.median(t["relax_launches"] for t in timings))
     peak = measured_peaks()
     if relax_ms >= merge_ms:
         kname, kms, launches_k = "k_relax", relax_ms, relax_launches
         alg = rows * relax_bytes_per_row(n, m)
         unit_note = f"12n+16m+4(n+1) bytes per row closure x {rows} rows"
     else:
-        kname, kms, launches_k = ("k_merge_stream" if cfg is SINGLE else "merge"), merge_ms, k - 1
+        kname, kms, launches_k = ("k_merge_stream16" if cfg is SINGLE else "merge"), merge_ms, k - 1
         alg = merge_bytes(n, k)
         unit_note = "12 bytes per (X,Y,v) triple x n(3^k-2^(k+1)+1)"
     achieved = alg / (kms / 1000.0) / 1e9
@@ -312,6 +308,8 @@ def run_single(args, dist: Dist, cfg: dict = SINGLE, cfg_name: str = SINGLE_NAME
            "phases_ms": {"merge": round(merge_ms, 3), "relax_incl_level1": round(relax_ms, 3),
                          "kernel": round(kernel_ms, 3)},
            "relax_sweeps_per_solve": int(statistics.median(t["relax_sweeps"] for t in timings)),
+           # levels (of k - 1 relaxed, k - 2 merged from level 3) that ran on 16-bit values; the table is int32
+           "levels_16bit": {"relax": timings[-1]["relax16_levels"], "merge": timings[-1]["merge16_levels"]},
            "gcell_per_s": round(((1 << k) * n) / (kernel_ms / 1000.0) / 1e9, 3),
            "merge_gbs_algorithmic": round(merge_bytes(n, k) / (merge_ms / 1000.0) / 1e9, 1),
            "relax_gbs_algorithmic": round(rows * relax_bytes_per_row(n, m) / (relax_ms / 1000.0) / 1e9, 1),

@@ -193,6 +193,7 @@ typedef struct emv_timing {
     int64_t launches;     /* kernel launches issued by the solve         */
     int64_t relax16_levels; /* levels relaxed with 16-bit records        */
     int64_t merge16_levels; /* levels merged from 16-bit staged rows     */
+    int64_t relax_launches; /* relaxation launches, level 1 included      */
 } emv_timing;
 
 /* Mirrors emv_kernel(n, m, k, c, C, q, kk, f_v, pos, adj, ...) (R:1966-2139)

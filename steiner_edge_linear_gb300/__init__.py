@@ -65,7 +65,7 @@ class _Timing(ctypes.Structure):
     _fields_ = [("zero_ms", ctypes.c_float), ("level1_ms", ctypes.c_float), ("merge_ms", ctypes.c_float),
                 ("relax_ms", ctypes.c_float), ("traceback_ms", ctypes.c_float), ("kernel_ms", ctypes.c_float),
                 ("relax_sweeps", ctypes.c_int64), ("launches", ctypes.c_int64), ("relax16_levels", ctypes.c_int64),
-                ("merge16_levels", ctypes.c_int64)]
+                ("merge16_levels", ctypes.c_int64), ("relax_launches", ctypes.c_int64)]
 
 
 class _Result(ctypes.Structure):

@@ -599,7 +599,7 @@ int run_dp(emv_ctx *c, int32_t n, const int32_t *row_ptr, const int2 *adj, int32
     // (level 1: its relaxation), all ones where the kernel does not record it.
     // They reach the host one level late, so no wait idles the device.
     uint32_t *d_max = (uint32_t *)c->lvlmax.ptr, *h_max = (uint32_t *)c->pinned + 64;
-    int64_t levels16 = 0, merges16 = 0;
+    int64_t levels16 = 0, merges16 = 0, relax_launches = 1;
     CUDA_TRY(cudaMemsetAsync(d_max, 0xff, sizeof(uint32_t) * (EMV_MAX_K + 1), st));
     CUDA_TRY(cudaMemsetAsync(d_max + 1, 0, sizeof(uint32_t), st));
 
@@ -642,6 +642,7 @@ int run_dp(emv_ctx *c, int32_t n, const int32_t *row_ptr, const int2 *adj, int32
             const int32_t rows = (int32_t)std::min<int64_t>(chunk, cnt - off);
             r = launch_relax(c, row_ptr, adj, n, ld, table, xs + b + off, rows, d_terms, 0, st, u16);
             if (r) return r;
+            relax_launches++;
         }
         CUDA_TRY(cudaEventRecord(E[ev++], st));  // relax end of level m
     }
@@ -680,6 +681,7 @@ int run_dp(emv_ctx *c, int32_t n, const int32_t *row_ptr, const int2 *adj, int32
         tm->relax_sweeps = (int64_t)ds.sweeps;
         tm->relax16_levels = levels16;
         tm->merge16_levels = merges16;
+        tm->relax_launches = relax_launches;
     }
     return EMV_OK;
 }
