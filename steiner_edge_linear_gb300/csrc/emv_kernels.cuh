@@ -325,10 +325,10 @@ __device__ __forceinline__ void merge_pair8(uint4 &a, const uint4 *__restrict__ 
 {
     const uint4 y = S4[(pr & 0xffffu) * 8];
     const uint4 z = S4[(pr >> 16) * 8];
-    a.x = __viaddmin_u16x2(y.x, z.x, a.x);
-    a.y = __viaddmin_u16x2(y.y, z.y, a.y);
-    a.z = __viaddmin_u16x2(y.z, z.z, a.z);
-    a.w = __viaddmin_u16x2(y.w, z.w, a.w);
+    a.x = addmin16(y.x, z.x, a.x);
+    a.y = addmin16(y.y, z.y, a.y);
+    a.z = addmin16(y.z, z.z, a.z);
+    a.w = addmin16(y.w, z.w, a.w);
 }
 
 __device__ __forceinline__ uint32_t pack16(int2 x)
