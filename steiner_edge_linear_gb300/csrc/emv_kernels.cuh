@@ -501,20 +501,29 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
     if (threadIdx.x == 0) s_chg = 0;
     __syncthreads();
     // Dense sweeps take every vertex (a vertex with no changed neighbour then
-    // selects no arc) and so need no neighbour flags from the sweep before:
-    // sweep s + 1 is dense when sweep s - 1 changed more than dense_min vertices.
+    // selects no arc) and so need no neighbour flags from the sweep before.
+    // Sweep s decides whether sweep s + 1 is dense before its own count of
+    // changed vertices is known: it predicts that count from the last two
+    // (their ratio continued while the counts fall) and makes sweep s + 1
+    // dense when the prediction exceeds dense_min.  A wrong guess costs time
+    // only: a sparse sweep's flags are written whenever the next one is sparse.
+    // Changed counts live in a ring of four words (sweep s: C_CNT0 + s % 4).
     bool dense = true;  // sweep 0: every vertex is active
     int32_t s = 0;
     for (; s < a.max_sweeps; s++) {
         uint8_t *cur = (s & 1) ? a.act1 : a.act0;
         uint8_t *nxt = (s & 1) ? a.act0 : a.act1;
-        const uint32_t prev_chg = s == 0 ? (uint32_t)n : vctrl[C_CNT0 + (s + 2) % 3];
-        const bool dense_next = prev_chg > (uint32_t)a.dense_min;
+        const uint32_t prev_chg = s == 0 ? (uint32_t)n : vctrl[C_CNT0 + (s + 3) % 4];
+        const uint32_t prev2_chg = s <= 1 ? (uint32_t)n : vctrl[C_CNT0 + (s + 2) % 4];
+        const uint32_t pred_chg = prev_chg < prev2_chg
+                                      ? (uint32_t)((uint64_t)prev_chg * prev_chg / prev2_chg)
+                                      : prev_chg;
+        const bool dense_next = pred_chg > (uint32_t)a.dense_min;
         // after a sweep that changed (almost) every vertex, pull every arc without reading stamps
         const bool pull_all = prev_chg >= (uint32_t)n - (uint32_t)n / 32;
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             vctrl[C_SLOT0 + (s + 1) % 3] = 0;
-            vctrl[C_CNT0 + (s + 1) % 3] = 0;
+            vctrl[C_CNT0 + (s + 1) % 4] = 0;
         }
         bool any = false;
         for (int32_t base = vbeg; base < vend; base += TASK_V) {
@@ -604,7 +613,7 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
         any = __syncthreads_or(any);
         if (threadIdx.x == 0) {
             if (any) vctrl[C_SLOT0 + s % 3] = 1;
-            if (s_chg) atomicAdd(a.ctrl + C_CNT0 + s % 3, s_chg);
+            if (s_chg) atomicAdd(a.ctrl + C_CNT0 + s % 4, s_chg);
             s_chg = 0;
         }
         if (!grid_barrier(a.ctrl, s_ok)) {
