@@ -647,21 +647,25 @@ __device__ void relax_load_records(const RelaxArgs &a, int32_t (*tile)[33])
     constexpr int R = 32 * VEC, NW = RELAX_THREADS / 32, PER = R / NW;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int32_t n = a.n, ntiles = (n + 31) >> 5;
-    for (int32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    // software pipeline: the next tile's row loads are in flight while this
+    // tile's records are written
+    int32_t x[PER], xh[U16 ? PER : 1];
+    auto fetch = [&](int32_t t) {
         const int32_t v = t * 32 + lane;
-        int32_t x[PER];
 #pragma unroll
         for (int q = 0; q < PER; q++) {
-            const int32_t row = warp + q * NW;
-            x[q] = relax_load_value<VEC, U16>(a, row, v);
-            if (U16) {
-                const int32_t hi = relax_load_value<VEC, U16>(a, row + R, v);
-                x[q] = (int32_t)(min((uint32_t)x[q], 0xffffu) | min((uint32_t)hi, 0xffffu) << 16);
-            }
+            x[q] = relax_load_value<VEC, U16>(a, warp + q * NW, v);
+            if (U16) xh[q] = relax_load_value<VEC, U16>(a, warp + q * NW + R, v);
         }
+    };
+    if (blockIdx.x < ntiles) fetch(blockIdx.x);
+    for (int32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
 #pragma unroll
-        for (int q = 0; q < PER; q++) tile[warp + q * NW][lane] = x[q];
+        for (int q = 0; q < PER; q++)
+            tile[warp + q * NW][lane] =
+                U16 ? (int32_t)(min((uint32_t)x[q], 0xffffu) | min((uint32_t)xh[U16 ? q : 0], 0xffffu) << 16) : x[q];
         __syncthreads();
+        if (t + (int32_t)gridDim.x < ntiles) fetch(t + gridDim.x);
         for (int vv = warp; vv < 32; vv += NW) {
             const int32_t v2 = t * 32 + vv;
             if (v2 < n)
@@ -686,14 +690,26 @@ __device__ void relax_store_records(const RelaxArgs &a, int32_t (*tile)[33])
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int32_t n = a.n, ntiles = (n + 31) >> 5, nrows = a.nrows;
     uint32_t vmax = 0;
-    for (int32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        for (int vv = warp; vv < 32; vv += NW) {
-            const int32_t v2 = t * 32 + vv;
+    // software pipeline: the next tile's record loads are in flight while
+    // this tile's rows are written
+    constexpr int VPW = 32 / NW;  // vertices of a tile per warp
+    int32_t y[VPW][VEC];
+    auto fetch = [&](int32_t t) {
 #pragma unroll
-            for (int g = 0; g < VEC; g++)
-                tile[g * 32 + lane][vv] = (v2 < n) ? __ldcg(a.scratch + (int64_t)v2 * R + g * 32 + lane) : INF;
+        for (int i = 0; i < VPW; i++) {
+            const int32_t v2 = t * 32 + warp + i * NW;
+#pragma unroll
+            for (int g = 0; g < VEC; g++) y[i][g] = (v2 < n) ? __ldcg(a.scratch + (int64_t)v2 * R + g * 32 + lane) : INF;
         }
+    };
+    if (blockIdx.x < ntiles) fetch(blockIdx.x);
+    for (int32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+#pragma unroll
+        for (int i = 0; i < VPW; i++)
+#pragma unroll
+            for (int g = 0; g < VEC; g++) tile[g * 32 + lane][warp + i * NW] = y[i][g];
         __syncthreads();
+        if (t + (int32_t)gridDim.x < ntiles) fetch(t + gridDim.x);
         const int32_t v = t * 32 + lane;
         if (v < n)
 #pragma unroll
