@@ -63,7 +63,7 @@ template <> struct IVec<2> {
 template <> struct IVec<4> {
     using T = int4;
 };
-struct int8v {  // 8 int32: a lane's share of a 256-row record
+struct int8v {  // 8 int32 words: a lane's share of a 1 KB record
     int4 a, b;
 };
 template <> struct IVec<8> {
