@@ -361,14 +361,15 @@ __global__ void __launch_bounds__(1024) k_merge_stream16(int32_t *__restrict__ t
     for (int32_t ph = 0; ph < nphase; ph++) {
         const MergePhase P = phases[ph];
         __syncthreads();
-        // staging: a warp takes 32 rows at a time, 8 row loads in flight per lane
+        // staging: a warp takes 32 rows at a time, 16 row loads in flight per lane
+        // (8: 1.4 % slower merge; 32 spills)
         for (int32_t c0 = warp * 32; c0 < P.nrows; c0 += nw * 32) {
             const uint32_t myr = c0 + lane < P.nrows ? __ldg(P.rows + c0 + lane) : 0u;
             const int32_t nr = min(32, P.nrows - c0);
-            for (int32_t j0 = 0; j0 < nr; j0 += 8) {
-                int2 x[8];
+            for (int32_t j0 = 0; j0 < nr; j0 += 16) {
+                int2 x[16];
 #pragma unroll
-                for (int u = 0; u < 8; u++) {
+                for (int u = 0; u < 16; u++) {
                     const uint32_t r = __shfl_sync(FULL, myr, j0 + u);
                     const int32_t *row = table + (int64_t)r * ld;
                     x[u] = make_int2(-1, -1);
@@ -378,7 +379,7 @@ __global__ void __launch_bounds__(1024) k_merge_stream16(int32_t *__restrict__ t
                     }
                 }
 #pragma unroll
-                for (int u = 0; u < 8; u++)
+                for (int u = 0; u < 16; u++)
                     if (j0 + u < nr) S[(c0 + j0 + u) * 32 + lane] = pack16(x[u]);
             }
         }
