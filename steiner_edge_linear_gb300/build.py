@@ -36,6 +36,7 @@ SOURCES = [
     "emv_server.cpp",
     "emv_noalloc.cu",
     "emv_bin.cpp",
+    "emv_plan.cpp",
 ]
 CLI_SOURCES = ["cli.cpp"]
 

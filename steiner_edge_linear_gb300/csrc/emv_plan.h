@@ -1,0 +1,40 @@
+// emv_plan.h -- host-side planning of the DP (no CUDA types): the subsets of
+// every level and the streamed merge's groups and phases.  Shared by the
+// library and the plan checks of the test suite.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <vector>
+
+// All non-empty subsets of {0..k-1} grouped by size, increasing within a
+// size -- the order Gosper's hack gives each level (R:2041-2046).  Level m
+// occupies xs[off[m], off[m + 1]).
+void subset_levels(int32_t k, std::vector<uint32_t> &xs, std::vector<int64_t> &off);
+
+namespace emv {
+
+// One phase of a group: offsets (in 32-bit words of the plan data) of its
+// staged rows, per-subset quad offsets and pair quads (posY | posZ << 16,
+// padded with (pad, pad), pad = nrows), and its staged row count (the pad
+// row is staged after them).
+struct HostPhase {
+    size_t rows_at, qoff_at, pairs_at;
+    int32_t nrows;
+};
+// One launch: subsets [x0, x0 + cnt) of a level, its shared memory and phases.
+struct HostGroup {
+    int64_t x0, cnt, smem;
+    std::vector<HostPhase> phases;
+};
+
+// Accumulator space of a group of g subsets, in 128-byte rows.
+int64_t stream_acc_rows(int64_t g);
+
+// Plans every level 2..k into data (all offsets relative to its start, blocks
+// read as uint4 16-byte aligned); plan[m] is empty for a level that cannot
+// be streamed within smem_bytes of shared memory.
+void plan_stream_levels(int32_t k, const std::vector<uint32_t> &xs, const std::vector<int64_t> &off,
+                        int64_t smem_bytes, std::vector<uint32_t> &data, std::vector<std::vector<HostGroup>> &plan);
+
+}  // namespace emv

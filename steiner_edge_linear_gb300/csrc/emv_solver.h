@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "emv_internal.h"
+#include "emv_plan.h"
 
 #define CUDA_TRY(x)                                                                                        \
     do {                                                                                                   \
@@ -86,7 +87,6 @@ struct emv_ctx {
     int32_t tune_rcap[BATCH_CLASSES] = {};
 };
 
-void subset_levels(int32_t k, std::vector<uint32_t> &xs, std::vector<int64_t> &off);
 int prepare_subsets(emv_ctx *c, int32_t k, cudaStream_t st);
 int reserve_relax(emv_ctx *c, int32_t n);
 int32_t relax_chunk_rows(const emv_ctx *c, int32_t n, bool u16);
