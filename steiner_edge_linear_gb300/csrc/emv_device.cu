@@ -177,6 +177,12 @@ int launch_relax(emv_ctx *c, const int32_t *row_ptr, const int2 *adj, int32_t n,
     a.dense_min = deg > 0 ? (int32_t)std::min<double>((double)n, (double)n * (1.0 - std::pow(0.1, 1.0 / deg))) : n;
     a.vmax = vmax;
     const int32_t words = u16 ? (nrows + 1) / 2 : nrows;  // int32 words a vertex record needs
+    // Without stamps a sweep pulls every arc, also from heads that did not
+    // change: worth it once most heads changed while the records are L2 hits
+    // (from 75 % of the vertices), only at 97 % when they stream from HBM.
+    const int64_t rec_words = words <= 32 ? 32 : words <= 64 ? 64 : words <= 128 ? 128 : 256;
+    const bool resident = (int64_t)n * rec_words * 4 <= c->l2_bytes * 3 / 4;
+    a.pull_all_min = n - n / (resident ? 4 : 32);
     const int vi = (words <= 32 ? 0 : words <= 64 ? 1 : words <= 128 ? 2 : 3) + (u16 ? 4 : 0);
     static const void *const fns[8] = {(const void *)k_relax<1>,       (const void *)k_relax<2>,
                                        (const void *)k_relax<4>,       (const void *)k_relax<8>,

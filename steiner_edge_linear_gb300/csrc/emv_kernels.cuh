@@ -42,6 +42,7 @@ struct RelaxArgs {
     int32_t max_sweeps;
     int32_t *stamp;         // n: last sweep in which the vertex changed (-1 none)
     int32_t dense_min;      // a sweep after one with more changed vertices takes every vertex
+    int32_t pull_all_min;   // a sweep after one with at least this many changed vertices reads no stamps
     uint32_t *vmax;         // if set: atomicMax of every value phase C writes
 };
 
@@ -522,8 +523,8 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
                                       ? (uint32_t)((uint64_t)prev_chg * prev_chg / prev2_chg)
                                       : prev_chg;
         const bool dense_next = pred_chg > (uint32_t)a.dense_min;
-        // after a sweep that changed (almost) every vertex, pull every arc without reading stamps
-        const bool pull_all = prev_chg >= (uint32_t)n - (uint32_t)n / 32;
+        // after a sweep that changed most vertices, pull every arc without reading stamps
+        const bool pull_all = prev_chg >= (uint32_t)a.pull_all_min;
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             vctrl[C_SLOT0 + (s + 1) % 3] = 0;
             vctrl[C_CNT0 + (s + 1) % 4] = 0;
