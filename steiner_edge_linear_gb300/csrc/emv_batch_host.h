@@ -32,5 +32,6 @@ int batch_pack(emv_ctx *c, const emv_instance *inst, const std::vector<int32_t> 
                BatchPack &pk);
 int batch_upload(emv_ctx *c, BatchPack &pk, cudaStream_t st);
 emv::BatchArgs batch_args(emv_ctx *c, const BatchPack &pk);
-int launch_batch(emv_ctx *c, const emv::BatchArgs &a, int32_t count, cudaStream_t st);
+// max_blocks > 0 caps the persistent grid (the autotuner's samples).
+int launch_batch(emv_ctx *c, const emv::BatchArgs &a, int32_t count, cudaStream_t st, int32_t max_blocks = 0);
 int batch_graph_launch(emv_ctx *c, const emv::BatchArgs &a, int32_t count, cudaStream_t st);
