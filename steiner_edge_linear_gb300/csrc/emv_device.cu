@@ -56,6 +56,14 @@ void dev_release(DevBuf &b)
 
 // ------------------------------------------------------------ context
 
+// Relaxation kernels by record width: k_relax<1, 2, 4, 5, 8> with 32-bit,
+// then with 16-bit records (32 * VEC words a vertex).
+static const void *const relax_fns[RELAX_VARIANTS] = {
+    (const void *)k_relax<1>,       (const void *)k_relax<2>,       (const void *)k_relax<4>,
+    (const void *)k_relax<5>,       (const void *)k_relax<8>,       (const void *)k_relax<1, true>,
+    (const void *)k_relax<2, true>, (const void *)k_relax<4, true>, (const void *)k_relax<5, true>,
+    (const void *)k_relax<8, true>};
+
 extern "C" int emv_create(emv_ctx **out, int32_t device)
 {
     if (!out) return emv_fail(EMV_ERR_BAD_INPUT, "null ctx pointer");
@@ -72,11 +80,7 @@ extern "C" int emv_create(emv_ctx **out, int32_t device)
     c->device = device;
     c->sms = prop.multiProcessorCount;
     c->l2_bytes = prop.l2CacheSize;
-    const void *relax_fns[8] = {(const void *)k_relax<1>,       (const void *)k_relax<2>,
-                                (const void *)k_relax<4>,       (const void *)k_relax<8>,
-                                (const void *)k_relax<1, true>, (const void *)k_relax<2, true>,
-                                (const void *)k_relax<4, true>, (const void *)k_relax<8, true>};
-    for (int i = 0; i < 8; i++) {
+    for (int i = 0; i < RELAX_VARIANTS; i++) {
         int per_sm = 0;
         CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, relax_fns[i], RELAX_THREADS, 0));
         c->relax_blocks_max[i] = std::max(1, per_sm) * c->sms;
@@ -180,15 +184,12 @@ int launch_relax(emv_ctx *c, const int32_t *row_ptr, const int2 *adj, int32_t n,
     // Without stamps a sweep pulls every arc, also from heads that did not
     // change: worth it once most heads changed while the records are L2 hits
     // (from 75 % of the vertices), only at 97 % when they stream from HBM.
-    const int64_t rec_words = words <= 32 ? 32 : words <= 64 ? 64 : words <= 128 ? 128 : 256;
+    const int wi = words <= 32 ? 0 : words <= 64 ? 1 : words <= 128 ? 2 : words <= 160 ? 3 : 4;
+    const int64_t rec_words = (int64_t)32 * (wi == 3 ? 5 : 1 << (wi < 3 ? wi : 3));
     const bool resident = (int64_t)n * rec_words * 4 <= c->l2_bytes * 3 / 4;
     a.pull_all_min = n - n / (resident ? 4 : 32);
-    const int vi = (words <= 32 ? 0 : words <= 64 ? 1 : words <= 128 ? 2 : 3) + (u16 ? 4 : 0);
-    static const void *const fns[8] = {(const void *)k_relax<1>,       (const void *)k_relax<2>,
-                                       (const void *)k_relax<4>,       (const void *)k_relax<8>,
-                                       (const void *)k_relax<1, true>, (const void *)k_relax<2, true>,
-                                       (const void *)k_relax<4, true>, (const void *)k_relax<8, true>};
-    const void *fn = fns[vi];
+    const int vi = wi + (u16 ? 5 : 0);
+    const void *fn = relax_fns[vi];
     // A warp per 8 vertices is enough; small graphs use fewer blocks (cheaper barriers).
     const int vpb = 8 * (RELAX_THREADS / 32);
     const int blocks = std::min(c->relax_blocks_max[vi], std::max(1, (n + vpb - 1) / vpb));
@@ -208,6 +209,21 @@ int32_t relax_chunk_rows(const emv_ctx *c, int32_t n, bool u16)
 {
     const int32_t rows = (int64_t)n * 512 <= c->l2_bytes * 3 / 4 ? 128 : CHUNK_ROWS;
     return u16 ? 2 * rows : rows;
+}
+
+// Rows per chunk for a level of cnt subsets.  A launch costs about the same
+// whatever its record width, so where 640-byte records (5/4 of the rows of
+// 512-byte ones) still fit three quarters of L2 and cut the level's launch
+// count, the level is cut into that many equal chunks.
+int32_t relax_chunk_rows_level(const emv_ctx *c, int32_t n, bool u16, int64_t cnt)
+{
+    const int32_t rows = relax_chunk_rows(c, n, u16);
+    const bool l2_fit = (int64_t)n * 512 <= c->l2_bytes * 3 / 4;
+    const int64_t rows5 = (int64_t)rows * 5 / 4;
+    if (!l2_fit || (int64_t)n * 640 > c->l2_bytes * 3 / 4) return rows;
+    const int64_t nch = (cnt + rows - 1) / rows, nch5 = (cnt + rows5 - 1) / rows5;
+    if (nch5 >= nch) return rows;
+    return (int32_t)((cnt + nch5 - 1) / nch5);
 }
 
 int reserve_relax(emv_ctx *c, int32_t n)
@@ -488,7 +504,7 @@ int run_dp(emv_ctx *c, int32_t n, const int32_t *row_ptr, const int2 *adj, int32
             u16 = (uint64_t)h_max[m - 1] + h_max[1] <= 32767;
         }
         levels16 += u16;
-        const int32_t chunk = relax_chunk_rows(c, n, u16);
+        const int32_t chunk = relax_chunk_rows_level(c, n, u16, cnt);
         for (int64_t off = 0; off < cnt; off += chunk) {
             const int32_t rows = (int32_t)std::min<int64_t>(chunk, cnt - off);
             r = launch_relax(c, row_ptr, adj, n, ld, table, xs + b + off, rows, d_terms, 0, st, u16);

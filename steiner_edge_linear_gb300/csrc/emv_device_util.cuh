@@ -63,6 +63,13 @@ template <> struct IVec<2> {
 template <> struct IVec<4> {
     using T = int4;
 };
+struct int5v {  // 5 int32 words: a lane's share of a 640-byte record
+    int4 a;
+    int32_t b;
+};
+template <> struct IVec<5> {
+    using T = int5v;
+};
 struct int8v {  // 8 int32 words: a lane's share of a 1 KB record
     int4 a, b;
 };
@@ -85,6 +92,9 @@ __device__ __forceinline__ bool vlt(int4 a, int4 b) { return a.x < b.x || a.y < 
 __device__ __forceinline__ int8v vmin(int8v x, int8v y) { return {vmin(x.a, y.a), vmin(x.b, y.b)}; }
 __device__ __forceinline__ int8v vadd(int8v x, int32_t w) { return {vadd(x.a, w), vadd(x.b, w)}; }
 __device__ __forceinline__ bool vlt(int8v x, int8v y) { return vlt(x.a, y.a) || vlt(x.b, y.b); }
+__device__ __forceinline__ int5v vmin(int5v x, int5v y) { return {vmin(x.a, y.a), min(x.b, y.b)}; }
+__device__ __forceinline__ int5v vadd(int5v x, int32_t w) { return {vadd(x.a, w), x.b + w}; }
+__device__ __forceinline__ bool vlt(int5v x, int5v y) { return vlt(x.a, y.a) || x.b < y.b; }
 // L2-only loads and stores of a lane's share (L1 may hold stale lines of records other SMs write)
 template <typename T> __device__ __forceinline__ T ldcg_v(const T *p) { return __ldcg(p); }
 template <> __device__ __forceinline__ int8v ldcg_v<int8v>(const int8v *p)
@@ -104,6 +114,7 @@ template <> __device__ __forceinline__ int32_t vsplat<int32_t>(int32_t x) { retu
 template <> __device__ __forceinline__ int2 vsplat<int2>(int32_t x) { return make_int2(x, x); }
 template <> __device__ __forceinline__ int4 vsplat<int4>(int32_t x) { return make_int4(x, x, x, x); }
 template <> __device__ __forceinline__ int8v vsplat<int8v>(int32_t x) { return {vsplat<int4>(x), vsplat<int4>(x)}; }
+template <> __device__ __forceinline__ int5v vsplat<int5v>(int32_t x) { return {vsplat<int4>(x), x}; }
 template <typename T> __device__ __forceinline__ T vinf() { return vsplat<T>(INF); }
 
 // min(a + b, c) per halfword of two packed 16-bit pairs (callers keep every
@@ -134,9 +145,39 @@ __device__ __forceinline__ int8v vaddmin16(int8v a, int32_t w2, int8v c)
 {
     return {vaddmin16(a.a, w2, c.a), vaddmin16(a.b, w2, c.b)};
 }
+__device__ __forceinline__ int5v vaddmin16(int5v a, int32_t w2, int5v c)
+{
+    return {vaddmin16(a.a, w2, c.a), vaddmin16(a.b, w2, c.b)};
+}
 __device__ __forceinline__ bool vne(int32_t a, int32_t b) { return a != b; }
 __device__ __forceinline__ bool vne(int2 a, int2 b) { return a.x != b.x || a.y != b.y; }
 __device__ __forceinline__ bool vne(int4 a, int4 b) { return a.x != b.x || a.y != b.y || a.z != b.z || a.w != b.w; }
 __device__ __forceinline__ bool vne(int8v x, int8v y) { return vne(x.a, y.a) || vne(x.b, y.b); }
+__device__ __forceinline__ bool vne(int5v x, int5v y) { return vne(x.a, y.a) || x.b != y.b; }
+
+// A lane's share of vertex v's record of 32 * VEC words (L2-only access).
+// VEC = 1, 2, 4, 8: words VEC * lane .. VEC * lane + VEC - 1; VEC = 5: words
+// 4 * lane .. 4 * lane + 3 and 128 + lane, so that both loads are aligned.
+template <int VEC>
+__device__ __forceinline__ typename IVec<VEC>::T rec_ld(const int32_t *scratch, int64_t v, int lane)
+{
+    return ldcg_v(reinterpret_cast<const typename IVec<VEC>::T *>(scratch + v * 32 * VEC) + lane);
+}
+template <> __device__ __forceinline__ int5v rec_ld<5>(const int32_t *scratch, int64_t v, int lane)
+{
+    const int32_t *r = scratch + v * 160;
+    return {__ldcg(reinterpret_cast<const int4 *>(r) + lane), __ldcg(r + 128 + lane)};
+}
+template <int VEC>
+__device__ __forceinline__ void rec_st(int32_t *scratch, int64_t v, int lane, typename IVec<VEC>::T x)
+{
+    stcg_v(reinterpret_cast<typename IVec<VEC>::T *>(scratch + v * 32 * VEC) + lane, x);
+}
+template <> __device__ __forceinline__ void rec_st<5>(int32_t *scratch, int64_t v, int lane, int5v x)
+{
+    int32_t *r = scratch + v * 160;
+    __stcg(reinterpret_cast<int4 *>(r) + lane, x.a);
+    __stcg(r + 128 + lane, x.b);
+}
 
 }  // namespace emv

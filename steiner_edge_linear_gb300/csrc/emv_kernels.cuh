@@ -488,7 +488,7 @@ template <int VEC, bool U16>
 __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
 {
     using V = typename IVec<VEC>::T;
-    constexpr int GROUP = VEC == 8 ? 2 : VEC == 4 ? 4 : 8;  // gathers in flight per group (2 KB for VEC >= 2)
+    constexpr int GROUP = VEC == 8 ? 2 : VEC >= 4 ? 4 : 8;  // gathers in flight per group
     constexpr int TASK_V = 8;
     const int lane = threadIdx.x & 31;
     const int32_t n = a.n;
@@ -497,7 +497,6 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
     // each warp owns a contiguous range of n / (warps) vertices, scanned TASK_V at a time
     const int32_t vbeg = (int32_t)((int64_t)n * gw / nwg), vend = (int32_t)((int64_t)n * (gw + 1) / nwg);
     volatile uint32_t *vctrl = a.ctrl;
-    const V *recs = reinterpret_cast<const V *>(a.scratch);  // vertex v: recs[v * 32 .. v * 32 + 31]
     __shared__ int2 s_arcs[RELAX_THREADS / 32][32];
     int2 *warcs = s_arcs[threadIdx.x >> 5];
     const unsigned lt = (1u << lane) - 1;
@@ -551,8 +550,7 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
             }
             for (;;) {
                 const int32_t vv = base + j;
-                V *mine = reinterpret_cast<V *>(a.scratch + (int64_t)vv * 32 * VEC) + lane;
-                const V old = ldcg_v(mine);
+                const V old = rec_ld<VEC>(a.scratch, vv, lane);
                 V acc = old;
                 for (int32_t e0 = beg;;) {
                     const unsigned sel = __ballot_sync(FULL, pull);
@@ -570,7 +568,7 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
                             const bool ok = i + g < cnt;
                             const int2 aw = warcs[(i + g) & 31];  // slots past cnt hold stale arcs: not used
                             wt[g] = ok ? aw.y : 0;
-                            val[g] = ok ? ldcg_v(recs + (int64_t)aw.x * 32 + lane) : vsplat<V>(U16 ? -1 : INF);
+                            val[g] = ok ? rec_ld<VEC>(a.scratch, aw.x, lane) : vsplat<V>(U16 ? -1 : INF);
                         }
 #pragma unroll
                         for (int g = 0; g < GROUP; g++)
@@ -601,7 +599,7 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
                     }
                 }
                 const bool dec = U16 ? vne(acc, old) : vlt(acc, old);
-                if (dec) stcg_v(mine, acc);
+                if (dec) rec_st<VEC>(a.scratch, vv, lane, acc);
                 if (__ballot_sync(FULL, dec)) {
                     any = true;
                     if (lane == 0) {

@@ -28,6 +28,7 @@ int dev_reserve(DevBuf &b, size_t bytes);
 void dev_release(DevBuf &b);
 
 constexpr int MAX_EVENTS = 64;
+constexpr int RELAX_VARIANTS = 10;  // relaxation kernels by record width (relax_fns)
 constexpr int BATCH_CLASSES = 12;  // (n bucket 0..3) x (k bucket 0..2)
 
 // One launch of the streamed merge: subsets [x0, x0 + cnt) of a level, its
@@ -52,7 +53,7 @@ struct KPlan {
 struct emv_ctx {
     int device = 0;
     int sms = 0;
-    int relax_blocks_max[8] = {};  // cooperative grid of k_relax<1>, <2>, <4>, <8>, then the 16-bit ones
+    int relax_blocks_max[RELAX_VARIANTS] = {};  // cooperative grid of each relaxation kernel
     int64_t l2_bytes = 0;
     int64_t sweep_limit = 0;       // relaxation sweeps per chunk, 0 = n + 1
     int32_t value_bits = 0;        // 0: 16-bit merge staging / relaxation records where bounded, 32: never
@@ -90,3 +91,4 @@ struct emv_ctx {
 int prepare_subsets(emv_ctx *c, int32_t k, cudaStream_t st);
 int reserve_relax(emv_ctx *c, int32_t n);
 int32_t relax_chunk_rows(const emv_ctx *c, int32_t n, bool u16);
+int32_t relax_chunk_rows_level(const emv_ctx *c, int32_t n, bool u16, int64_t cnt);

@@ -211,6 +211,26 @@ def test_wide_records_and_partial_merge_block_equal_32_bit_values(emv):
     assert a.cost == b.cost and np.array_equal(a.table, b.table)
 
 
+def test_640_byte_records_match_oracle(emv, orc):
+    """k = 12 with weights up to 8000 keeps 32-bit values: levels 5..7 (792,
+    924, 792 subsets) relax in 5, 6 and 5 chunks of 640-byte records instead
+    of 7, 8 and 7 of 512 bytes.  Whole table against the oracle, and the
+    launch count of that chunk rule."""
+    inst = emv.StpInstance.regular(2000, 6, 1, 8000, 12, 606)
+    csr = emv.Csr.from_stp(inst)
+    want, want_cost = orc.emv_table(csr.n, csr.row_ptr, csr.col, csr.w, csr.terminals, threads=8)
+    with emv.Solver(0) as s:
+        res = s.solve(csr, tree=True, table=True)
+    assert res.timing["relax16_levels"] == 0
+    # level 1, then per level m: 66 -> 1, 220 -> 2, 495 -> 4, 792 -> 5, 924 -> 6, 792 -> 5, 495 -> 4, 220 -> 2,
+    # 66, 12, 1 -> 1 each
+    assert res.timing["relax_launches"] == 1 + 1 + 2 + 4 + 5 + 6 + 5 + 4 + 2 + 1 + 1 + 1
+    assert res.cost == want_cost
+    mism = np.argwhere(res.table != want)
+    assert mism.size == 0, f"{len(mism)} cells differ, first (X, v) = {mism[:5].tolist()}"
+    check_tree(csr.n, inst.edges, res.tree, csr.terminals, res.cost)
+
+
 def test_bad_inputs_report_status(emv, solver):
     disc = emv.StpInstance.from_text(
         "section graph\nnodes 4\nedges 2\ne 1 2 3\ne 3 4 5\nend\nsection terminals\nterminals 2\nt 1\nt 3\nend\n")
