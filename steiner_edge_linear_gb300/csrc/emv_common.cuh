@@ -11,7 +11,7 @@ namespace emv {
 constexpr int32_t INF = EMV_INF32;
 constexpr unsigned FULL = 0xffffffffu;
 constexpr int RELAX_THREADS = 512;       // 16 warps; a warp takes 8 vertices at a time
-constexpr int CHUNK_ROWS = 256;          // most rows per relaxation chunk (32 lanes x 8 int32)
+constexpr int CHUNK_ROWS = 256;          // most int32 rows per relaxation chunk (1 KB records: 32 lanes x 8 words)
 constexpr uint32_t SPIN_LIMIT = 1u << 22;  // grid-barrier spin iterations (~1 s with nanosleep)
 constexpr int TB_STACK = 64;
 

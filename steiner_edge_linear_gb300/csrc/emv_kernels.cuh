@@ -11,7 +11,7 @@
 //   k_merge, k_merge_smem, k_merge_stream, k_merge_stream16
 //                 subset merge of one level           R:2068-2107
 //   k_relax<VEC, U16>  multi-source closure of <= 32*VEC rows (64*VEC with
-//                 16-bit records)                     R:2109-2130, R:1762-1880
+//                 16-bit records; VEC = 1, 2, 4, 5, 8) R:2109-2130, R:1762-1880
 //                 (also the k level-1 SSSPs,          R:1988-2031)
 //   k_traceback   tree recovery by recomputation      R:1907-1944
 #pragma once
