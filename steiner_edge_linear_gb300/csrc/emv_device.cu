@@ -123,7 +123,7 @@ extern "C" int emv_destroy(emv_ctx *c)
     if (!c) return EMV_OK;
     cudaSetDevice(c->device);
     cudaDeviceSynchronize();
-    for (DevBuf *b : {&c->ctrl, &c->stat, &c->lvlmax, &c->scratch, &c->act, &c->adj, &c->stamp, &c->terms, &c->g_row,
+    for (DevBuf *b : {&c->ctrl, &c->stat, &c->lvlmax, &c->shadow, &c->scratch, &c->act, &c->adj, &c->stamp, &c->terms, &c->g_row,
                       &c->g_col, &c->g_w, &c->table, &c->tb_edges, &c->tb_out, &c->tb_work})
         dev_release(*b);
     for (KPlan *p : c->kplans) {
@@ -155,7 +155,7 @@ static int grid_for(int64_t work, int threads, int cap)
 // value written.
 int launch_relax(emv_ctx *c, const int32_t *row_ptr, const int2 *adj, int32_t n, int64_t ld, int32_t *table,
                  const uint32_t *rows, int32_t nrows, const int32_t *terms, int32_t level1, cudaStream_t st,
-                 bool u16 = false, uint32_t *vmax = nullptr)
+                 bool u16 = false, uint32_t *vmax = nullptr, uint16_t *shadow = nullptr, int64_t shadow_ld = 0)
 {
     RelaxArgs a;
     a.stamp = (int32_t *)c->stamp.ptr;
@@ -180,6 +180,8 @@ int launch_relax(emv_ctx *c, const int32_t *row_ptr, const int2 *adj, int32_t n,
     const double deg = (double)c->relax_arcs / (double)n;
     a.dense_min = deg > 0 ? (int32_t)std::min<double>((double)n, (double)n * (1.0 - std::pow(0.1, 1.0 / deg))) : n;
     a.vmax = vmax;
+    a.shadow = shadow;
+    a.shadow_ld = shadow_ld;
     const int32_t words = u16 ? (nrows + 1) / 2 : nrows;  // int32 words a vertex record needs
     // Without stamps a sweep pulls every arc, also from heads that did not
     // change: worth it once most heads changed while the records are L2 hits
@@ -384,7 +386,7 @@ static cudaError_t merge_smem_launch(emv_ctx *c, int32_t *table, int64_t ld, int
 // Merge of level m: the shared-memory kernel with the widest vertex block
 // whose staging fits, else the direct kernel (k above MERGE_SMEM_KMAX).
 int launch_merge(emv_ctx *c, int32_t *table, int64_t ld, int32_t n, int32_t k, int32_t m, const int32_t *d_terms,
-                 cudaStream_t st, bool u16 = false)
+                 cudaStream_t st, bool u16 = false, const uint16_t *shadow = nullptr, int64_t shadow_ld = 0)
 {
     if (!c->merge_attr) {
         const void *fns[6] = {(const void *)k_merge_smem<32>, (const void *)k_merge_smem<16>,
@@ -415,7 +417,8 @@ int launch_merge(emv_ctx *c, int32_t *table, int64_t ld, int32_t n, int32_t k, i
             const MergePhase *pg = (const MergePhase *)c->kp->mstream_phases.ptr + g.phase_off;
             if (u16)
                 k_merge_stream16<<<(unsigned)((n + 63) / 64), 1024, (size_t)g.smem, st>>>(
-                    table, ld, n, xg, (int32_t)g.cnt, pg, (int32_t)g.nphase, d_terms, k, (uint32_t *)c->lvlmax.ptr + m);
+                    table, ld, n, xg, (int32_t)g.cnt, pg, (int32_t)g.nphase, d_terms, k, (uint32_t *)c->lvlmax.ptr + m,
+                    shadow, shadow_ld);
             else
                 k_merge_stream<<<(unsigned)((n + 31) / 32), 1024, (size_t)g.smem, st>>>(
                     table, ld, n, xg, (int32_t)g.cnt, pg, (int32_t)g.nphase, d_terms, k, (uint32_t *)c->lvlmax.ptr + m);
@@ -466,12 +469,27 @@ int run_dp(emv_ctx *c, int32_t n, const int32_t *row_ptr, const int2 *adj, int32
     // (level 1: its relaxation), all ones where the kernel does not record it.
     // They reach the host one level late, so no wait idles the device.
     uint32_t *d_max = (uint32_t *)c->lvlmax.ptr, *h_max = (uint32_t *)c->pinned + 64;
+    // 16-bit shadow of the relaxed rows (stride a multiple of 64 vertices):
+    // the 16-bit merge stages from it with 16-byte asynchronous copies.  Taken
+    // when 16-bit values are allowed and the memory is free (with 1 GiB to
+    // spare); without it the merge packs the int32 rows itself.
+    uint16_t *shadow = nullptr;
+    const int64_t sld = ((int64_t)n + 63) / 64 * 64;
+    if (c->value_bits == 0 && k >= 3) {
+        const size_t need = sizeof(uint16_t) * (size_t)sld << k;
+        size_t fr = 0, tot = 0;
+        if (c->shadow.bytes >= need ||
+            (cudaMemGetInfo(&fr, &tot) == cudaSuccess && need + ((size_t)1 << 30) < fr && dev_reserve(c->shadow, need) == EMV_OK))
+            shadow = (uint16_t *)c->shadow.ptr;
+        cudaGetLastError();
+    }
     int64_t levels16 = 0, merges16 = 0, relax_launches = 1;
     CUDA_TRY(cudaMemsetAsync(d_max, 0xff, sizeof(uint32_t) * (EMV_MAX_K + 1), st));
     CUDA_TRY(cudaMemsetAsync(d_max + 1, 0, sizeof(uint32_t), st));
 
     // Level 1: k single-source closures (R:1988-2031).
-    r = launch_relax(c, row_ptr, adj, n, ld, table, xs + c->kp->xs_off[1], k, d_terms, 1, st, false, d_max + 1);
+    r = launch_relax(c, row_ptr, adj, n, ld, table, xs + c->kp->xs_off[1], k, d_terms, 1, st, false, d_max + 1,
+                     shadow, sld);
     if (r) return r;
     CUDA_TRY(cudaEventRecord(E[ev++], st));  // 2: after level 1
     CUDA_TRY(cudaMemcpyAsync(h_max + 1, d_max + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
@@ -489,7 +507,7 @@ int run_dp(emv_ctx *c, int32_t n, const int32_t *row_ptr, const int2 *adj, int32
             for (int32_t j = 1; 2 * j <= m; j++) worst = std::max<uint64_t>(worst, (uint64_t)h_max[j] + h_max[m - j]);
             m16 = worst <= 65533;
         }
-        r = launch_merge(c, table, ld, n, k, m, d_terms, st, m16);
+        r = launch_merge(c, table, ld, n, k, m, d_terms, st, m16, shadow, sld);
         if (r) return r;
         merges16 += c->merge16_last;
         CUDA_TRY(cudaEventRecord(E[ev++], st));  // merge end of level m
@@ -507,7 +525,8 @@ int run_dp(emv_ctx *c, int32_t n, const int32_t *row_ptr, const int2 *adj, int32
         const int32_t chunk = relax_chunk_rows_level(c, n, u16, cnt);
         for (int64_t off = 0; off < cnt; off += chunk) {
             const int32_t rows = (int32_t)std::min<int64_t>(chunk, cnt - off);
-            r = launch_relax(c, row_ptr, adj, n, ld, table, xs + b + off, rows, d_terms, 0, st, u16);
+            r = launch_relax(c, row_ptr, adj, n, ld, table, xs + b + off, rows, d_terms, 0, st, u16, nullptr, shadow,
+                             sld);
             if (r) return r;
             relax_launches++;
         }

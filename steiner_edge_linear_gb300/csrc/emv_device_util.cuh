@@ -50,6 +50,12 @@ __device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)), "l"(gmem)
                  : "memory");
 }
+// 16-byte variant (both addresses 16-byte aligned; L2 only).
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)), "l"(gmem)
+                 : "memory");
+}
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 // Vector of VEC int32 (one lane's share of a vertex record).

@@ -44,6 +44,8 @@ struct RelaxArgs {
     int32_t dense_min;      // a sweep after one with more changed vertices takes every vertex
     int32_t pull_all_min;   // a sweep after one with at least this many changed vertices reads no stamps
     uint32_t *vmax;         // if set: atomicMax of every value phase C writes
+    uint16_t *shadow;       // if set: phase C also writes min(value, 0xffff) to shadow[X * shadow_ld + v]
+    int64_t shadow_ld;
 };
 
 __global__ void k_fill(int32_t *__restrict__ p, int64_t count, int32_t value)
@@ -343,7 +345,8 @@ __global__ void __launch_bounds__(1024) k_merge_stream16(int32_t *__restrict__ t
                                                          const uint32_t *__restrict__ xs_level, int32_t cnt,
                                                          const MergePhase *__restrict__ phases, int32_t nphase,
                                                          const int32_t *__restrict__ terms, int32_t k,
-                                                         uint32_t *__restrict__ level_max)
+                                                         uint32_t *__restrict__ level_max,
+                                                         const uint16_t *__restrict__ shadow, int64_t sld)
 {
     extern __shared__ __align__(16) uint32_t sm[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -362,8 +365,24 @@ __global__ void __launch_bounds__(1024) k_merge_stream16(int32_t *__restrict__ t
     for (int32_t ph = 0; ph < nphase; ph++) {
         const MergePhase P = phases[ph];
         __syncthreads();
-        // staging: a warp takes 32 rows at a time, 16 row loads in flight per lane
-        // (8: 1.4 % slower merge; 32 spills)
+        if (shadow) {
+            // 16-bit shadow rows (stride sld, a multiple of 64 vertices): eight
+            // lanes copy a staged row with 16-byte cp.async, all of a warp's
+            // rows in flight; vertices past n are read but never stored
+            const int sub = lane >> 3, sl = lane & 7;
+            for (int32_t c0 = warp * 32; c0 < P.nrows; c0 += nw * 32) {
+                const uint32_t myr = c0 + lane < P.nrows ? __ldg(P.rows + c0 + lane) : 0u;
+                const int32_t nr = min(32, P.nrows - c0);
+                for (int32_t j0 = 0; j0 < nr; j0 += 4) {
+                    const int32_t j = j0 + sub;
+                    const uint32_t r = __shfl_sync(FULL, myr, j & 31);
+                    if (j < nr) cp_async16(S + (c0 + j) * 32 + sl * 4, shadow + (int64_t)r * sld + v0 + sl * 8);
+                }
+            }
+            cp_async_wait_all();
+        } else
+        // staging through registers: a warp takes 32 rows at a time, 16 row
+        // loads in flight per lane (8: 1.4 % slower merge; 32 spills)
         for (int32_t c0 = warp * 32; c0 < P.nrows; c0 += nw * 32) {
             const uint32_t myr = c0 + lane < P.nrows ? __ldg(P.rows + c0 + lane) : 0u;
             const int32_t nr = min(32, P.nrows - c0);
@@ -721,10 +740,20 @@ __device__ void relax_store_records(const RelaxArgs &a, int32_t (*tile)[33])
                 if (U16) {
                     const uint32_t lo = word & 0xffffu, hi = word >> 16;
                     const int32_t xlo = lo == 0xffffu ? INF : (int32_t)lo, xhi = hi == 0xffffu ? INF : (int32_t)hi;
-                    if (row < nrows) a.table[(int64_t)__ldg(a.rows + row) * a.ld + v] = xlo;
-                    if (row + R < nrows) a.table[(int64_t)__ldg(a.rows + row + R) * a.ld + v] = xhi;
+                    if (row < nrows) {
+                        const int64_t X = __ldg(a.rows + row);
+                        a.table[X * a.ld + v] = xlo;
+                        if (a.shadow) a.shadow[X * a.shadow_ld + v] = (uint16_t)lo;
+                    }
+                    if (row + R < nrows) {
+                        const int64_t X = __ldg(a.rows + row + R);
+                        a.table[X * a.ld + v] = xhi;
+                        if (a.shadow) a.shadow[X * a.shadow_ld + v] = (uint16_t)hi;
+                    }
                 } else if (row < nrows) {
-                    a.table[(int64_t)__ldg(a.rows + row) * a.ld + v] = (int32_t)word;
+                    const int64_t X = __ldg(a.rows + row);
+                    a.table[X * a.ld + v] = (int32_t)word;
+                    if (a.shadow) a.shadow[X * a.shadow_ld + v] = (uint16_t)min(word, 0xffffu);
                     vmax = max(vmax, word);
                 }
             }

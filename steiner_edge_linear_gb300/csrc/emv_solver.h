@@ -61,6 +61,7 @@ struct emv_ctx {
     int64_t relax_arcs = 0;       // arcs of the graph being relaxed (dense-sweep threshold)
     DevBuf ctrl, stat;             // relaxation barrier words, solve status
     DevBuf lvlmax;                 // per level: largest value its merge (level 1: relaxation) wrote
+    DevBuf shadow;                 // 16-bit copy of the relaxed rows (the 16-bit merge's staging source)
     cudaEvent_t evmax[EMV_MAX_K + 1] = {};  // level m's maximum has reached the pinned buffer
     DevBuf scratch, act;           // vertex-major chunk buffer, active flags
     DevBuf stamp;                  // per vertex: last sweep in which it changed
