@@ -176,9 +176,10 @@ int emv_set_sweep_limit(emv_ctx *ctx, int64_t limit);
  * 0 (the default) stages a level's merge rows as 16-bit values when every
  * sum of two of them is provably at most 65533, and relaxes a level with
  * 16-bit records when its values are provably at most 32767 (twice the rows
- * per chunk at the same bytes); 32 always keeps 32 bits.  The table is int32
- * and identical either way.  No reference counterpart (it works on the int32
- * table directly). */
+ * per chunk at the same bytes); 32 always keeps 32 bits.  With 0 the context
+ * also keeps a 16-bit shadow of the table (2 bytes per cell) when that
+ * memory is free.  The table is int32 and identical either way.  No
+ * reference counterpart (it works on the int32 table directly). */
 int emv_set_value_bits(emv_ctx *ctx, int32_t bits);
 
 /* Per-phase device times of the last solve (CUDA events, ms). */
