@@ -475,7 +475,7 @@ int run_dp(emv_ctx *c, int32_t n, const int32_t *row_ptr, const int2 *adj, int32
     // spare); without it the merge packs the int32 rows itself.
     uint16_t *shadow = nullptr;
     const int64_t sld = ((int64_t)n + 63) / 64 * 64;
-    if (c->value_bits == 0 && k >= 3) {
+    if (c->value_bits == 0 && k >= 3 && k <= MERGE_SMEM_KMAX) {  // the streamed merge's k
         const size_t need = sizeof(uint16_t) * (size_t)sld << k;
         size_t fr = 0, tot = 0;
         if (c->shadow.bytes >= need ||
