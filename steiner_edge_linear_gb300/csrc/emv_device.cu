@@ -202,30 +202,11 @@ int launch_relax(emv_ctx *c, const int32_t *row_ptr, const int2 *adj, int32_t n,
     return EMV_OK;
 }
 
-// Rows per relaxation chunk: 512-byte vertex records while they fit in three
-// quarters of L2 (the sweeps' gathers are then L2 hits and larger records
-// only add bytes per sweep), else 1 KB ones, which halve the sweeps of the
-// graphs whose records stream from HBM anyway.  16-bit records hold twice
-// the rows.
-int32_t relax_chunk_rows(const emv_ctx *c, int32_t n, bool u16)
-{
-    const int32_t rows = (int64_t)n * 512 <= c->l2_bytes * 3 / 4 ? 128 : CHUNK_ROWS;
-    return u16 ? 2 * rows : rows;
-}
+int32_t relax_chunk_rows(const emv_ctx *c, int32_t n, bool u16) { return relax_rows_per_chunk(n, c->l2_bytes, u16); }
 
-// Rows per chunk for a level of cnt subsets.  A launch costs about the same
-// whatever its record width, so where 640-byte records (5/4 of the rows of
-// 512-byte ones) still fit three quarters of L2 and cut the level's launch
-// count, the level is cut into that many equal chunks.
 int32_t relax_chunk_rows_level(const emv_ctx *c, int32_t n, bool u16, int64_t cnt)
 {
-    const int32_t rows = relax_chunk_rows(c, n, u16);
-    const bool l2_fit = (int64_t)n * 512 <= c->l2_bytes * 3 / 4;
-    const int64_t rows5 = (int64_t)rows * 5 / 4;
-    if (!l2_fit || (int64_t)n * 640 > c->l2_bytes * 3 / 4) return rows;
-    const int64_t nch = (cnt + rows - 1) / rows, nch5 = (cnt + rows5 - 1) / rows5;
-    if (nch5 >= nch) return rows;
-    return (int32_t)((cnt + nch5 - 1) / nch5);
+    return relax_rows_per_level_chunk(n, c->l2_bytes, u16, cnt);
 }
 
 int reserve_relax(emv_ctx *c, int32_t n)

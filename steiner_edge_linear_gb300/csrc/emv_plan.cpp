@@ -18,6 +18,23 @@ void subset_levels(int32_t k, std::vector<uint32_t> &xs, std::vector<int64_t> &o
 
 namespace emv {
 
+int32_t relax_rows_per_chunk(int64_t n, int64_t l2_bytes, bool u16)
+{
+    // 256 int32 words a vertex is the relaxation scratch's capacity (CHUNK_ROWS)
+    const int32_t rows = n * 512 <= l2_bytes * 3 / 4 ? 128 : 256;
+    return u16 ? 2 * rows : rows;
+}
+
+int32_t relax_rows_per_level_chunk(int64_t n, int64_t l2_bytes, bool u16, int64_t cnt)
+{
+    const int32_t rows = relax_rows_per_chunk(n, l2_bytes, u16);
+    const int64_t rows5 = (int64_t)rows * 5 / 4;
+    if (n * 512 > l2_bytes * 3 / 4 || n * 640 > l2_bytes * 3 / 4) return rows;
+    const int64_t nch = (cnt + rows - 1) / rows, nch5 = (cnt + rows5 - 1) / rows5;
+    if (nch5 >= nch) return rows;
+    return (int32_t)((cnt + nch5 - 1) / nch5);
+}
+
 // Accumulator space of a streamed-merge group of g subsets, in 128-byte rows:
 // one per subset, two where the 16-bit kernel keeps one uint32 per vertex
 // (g <= 64: its 128 quarter-warps then split each subset's pairs).

@@ -14,6 +14,18 @@ void subset_levels(int32_t k, std::vector<uint32_t> &xs, std::vector<int64_t> &o
 
 namespace emv {
 
+// Rows per relaxation chunk of an n-vertex graph: 512-byte vertex records
+// while they fit in three quarters of L2 (the sweeps' gathers are then L2
+// hits and larger records only add bytes per sweep), else 1 KB ones, which
+// halve the sweeps of graphs whose records stream from HBM anyway; 16-bit
+// records hold twice the rows.
+int32_t relax_rows_per_chunk(int64_t n, int64_t l2_bytes, bool u16);
+// Rows per chunk for a level of cnt subsets.  A launch costs about the same
+// whatever its record width, so where 640-byte records (5/4 of the rows of
+// 512-byte ones) still fit three quarters of L2 and cut the level's launch
+// count, the level is cut into that many equal chunks.
+int32_t relax_rows_per_level_chunk(int64_t n, int64_t l2_bytes, bool u16, int64_t cnt);
+
 // One phase of a group: offsets (in 32-bit words of the plan data) of its
 // staged rows, per-subset quad offsets and pair quads (posY | posZ << 16,
 // padded with (pad, pad), pad = nrows), and its staged row count (the pad

@@ -13,6 +13,7 @@
 #include <cstdlib>
 #include <map>
 #include <set>
+#include <string>
 #include <utility>
 
 using namespace emv;
@@ -23,8 +24,41 @@ static int fail(const char *what, int k, int m)
     return 1;
 }
 
+// The relaxation chunk rule: chunks never exceed the kernels' record widths
+// (160 words with L2-resident records, 256 otherwise), cover a level in the
+// fewest launches the rule allows, and match worked cases.
+static int check_chunks()
+{
+    const int64_t l2 = 126ll << 20;
+    auto expect = [&](int64_t n, bool u16, int64_t cnt, int32_t rows) {
+        const int32_t got = relax_rows_per_level_chunk(n, l2, u16, cnt);
+        if (got != rows) std::printf("FAIL chunks n=%lld u16=%d cnt=%lld: %d rows, want %d\n", (long long)n, (int)u16,
+                                     (long long)cnt, got, rows);
+        return got == rows;
+    };
+    bool ok = expect(100000, true, 792, 264) && expect(100000, true, 924, 308) && expect(100000, true, 495, 256) &&
+              expect(100000, true, 220, 256) && expect(100000, false, 924, 154) && expect(100000, false, 792, 159) &&
+              expect(100000, false, 495, 128) && expect(1 << 20, true, 3432, 512) && expect(1 << 20, false, 3432, 256) &&
+              expect(160000, true, 792, 256);
+    for (int64_t n : {64ll, 1000ll, 100000ll, 150000ll, 200000ll, 1ll << 20})
+        for (int u = 0; u < 2 && ok; u++)
+            for (int64_t cnt = 1; cnt <= 3432 && ok; cnt++) {
+                const int32_t rows = relax_rows_per_level_chunk(n, l2, u != 0, cnt);
+                const int64_t words = u ? (rows + 1) / 2 : rows;
+                const bool resident = n * 512 <= l2 * 3 / 4;
+                const int64_t base = relax_rows_per_chunk(n, l2, u != 0);
+                if (rows < 1 || words > (resident ? 160 : 256) || (cnt + rows - 1) / rows > (cnt + base - 1) / base) {
+                    std::printf("FAIL chunks n=%lld u16=%d cnt=%lld: %d rows\n", (long long)n, u, (long long)cnt, rows);
+                    ok = false;
+                }
+            }
+    if (ok) std::printf("ok chunks\n");
+    return ok ? 0 : 1;
+}
+
 int main(int argc, char **argv)
 {
+    if (argc == 2 && std::string(argv[1]) == "chunks") return check_chunks();
     if (argc < 3) return 2;
     const int k = std::atoi(argv[1]);
     const int64_t smem = std::atoll(argv[2]);

@@ -32,6 +32,13 @@ def test_merge_plan_covers_every_pair_once(checker, k):
     assert out.stdout.startswith(f"ok k={k} streamed_levels={k - 1} "), out.stdout
 
 
+def test_relaxation_chunk_rule(checker):
+    """Chunk rows per level: within the kernels' record widths, never more
+    launches than 512-byte records take, and the worked n = 1e5 / 2^20 cases."""
+    out = subprocess.run([checker, "chunks"], capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0 and out.stdout.startswith("ok chunks"), out.stdout + out.stderr
+
+
 def test_smaller_budget_still_covers(checker):
     """A quarter of the shared memory forces more groups and row tiles."""
     out = subprocess.run([checker, "12", str(STREAM_SMEM_BYTES // 4)], capture_output=True, text=True, timeout=600)
