@@ -155,7 +155,8 @@ static int grid_for(int64_t work, int threads, int cap)
 // value written.
 int launch_relax(emv_ctx *c, const int32_t *row_ptr, const int2 *adj, int32_t n, int64_t ld, int32_t *table,
                  const uint32_t *rows, int32_t nrows, const int32_t *terms, int32_t level1, cudaStream_t st,
-                 bool u16 = false, uint32_t *vmax = nullptr, uint16_t *shadow = nullptr, int64_t shadow_ld = 0)
+                 bool u16 = false, uint32_t *vmax = nullptr, uint16_t *shadow = nullptr, int64_t shadow_ld = 0,
+                 bool init_shadow = false)
 {
     RelaxArgs a;
     a.stamp = (int32_t *)c->stamp.ptr;
@@ -182,6 +183,7 @@ int launch_relax(emv_ctx *c, const int32_t *row_ptr, const int2 *adj, int32_t n,
     a.vmax = vmax;
     a.shadow = shadow;
     a.shadow_ld = shadow_ld;
+    a.init_shadow = init_shadow && u16 && shadow;
     const int32_t words = u16 ? (nrows + 1) / 2 : nrows;  // int32 words a vertex record needs
     // Without stamps a sweep pulls every arc, also from heads that did not
     // change: worth it once most heads changed while the records are L2 hits
@@ -367,7 +369,8 @@ static cudaError_t merge_smem_launch(emv_ctx *c, int32_t *table, int64_t ld, int
 // Merge of level m: the shared-memory kernel with the widest vertex block
 // whose staging fits, else the direct kernel (k above MERGE_SMEM_KMAX).
 int launch_merge(emv_ctx *c, int32_t *table, int64_t ld, int32_t n, int32_t k, int32_t m, const int32_t *d_terms,
-                 cudaStream_t st, bool u16 = false, const uint16_t *shadow = nullptr, int64_t shadow_ld = 0)
+                 cudaStream_t st, bool u16 = false, const uint16_t *shadow = nullptr, int64_t shadow_ld = 0,
+                 uint16_t *shadow_out = nullptr)
 {
     if (!c->merge_attr) {
         const void *fns[6] = {(const void *)k_merge_smem<32>, (const void *)k_merge_smem<16>,
@@ -399,7 +402,7 @@ int launch_merge(emv_ctx *c, int32_t *table, int64_t ld, int32_t n, int32_t k, i
             if (u16)
                 k_merge_stream16<<<(unsigned)((n + 63) / 64), 1024, (size_t)g.smem, st>>>(
                     table, ld, n, xg, (int32_t)g.cnt, pg, (int32_t)g.nphase, d_terms, k, (uint32_t *)c->lvlmax.ptr + m,
-                    shadow, shadow_ld);
+                    shadow, shadow_ld, shadow_out);
             else
                 k_merge_stream<<<(unsigned)((n + 31) / 32), 1024, (size_t)g.smem, st>>>(
                     table, ld, n, xg, (int32_t)g.cnt, pg, (int32_t)g.nphase, d_terms, k, (uint32_t *)c->lvlmax.ptr + m);
@@ -481,24 +484,29 @@ int run_dp(emv_ctx *c, int32_t n, const int32_t *row_ptr, const int2 *adj, int32
         // 16-bit merge staging when every sum of two lower-level values is
         // at most 65533 (M(j) bounds level j's values); from level 3 on, where
         // waiting for level m-1's maximum leaves its relaxation queued.
-        bool m16 = false;
+        // 16-bit relaxation records when M(m-1) + M(1) <= 32767: the split
+        // {X \ t, t} bounds every merged value of level m by it, and relaxed
+        // values never exceed merged ones (level 2 decides after its merge is
+        // queued, so that no wait idles the device).
+        bool m16 = false, u16 = false;
         if (c->value_bits == 0 && m >= 3) {
             CUDA_TRY(cudaEventSynchronize(c->evmax[m - 1]));
             uint64_t worst = 0;
             for (int32_t j = 1; 2 * j <= m; j++) worst = std::max<uint64_t>(worst, (uint64_t)h_max[j] + h_max[m - j]);
             m16 = worst <= 65533;
+            u16 = (uint64_t)h_max[m - 1] + h_max[1] <= 32767;
         }
-        r = launch_merge(c, table, ld, n, k, m, d_terms, st, m16, shadow, sld);
+        // A level merged and relaxed in 16 bits keeps its merged rows only in
+        // the shadow: the relaxation reads them there and writes the int32 rows.
+        const bool via_shadow = m16 && u16 && shadow;
+        r = launch_merge(c, table, ld, n, k, m, d_terms, st, m16, shadow, sld, via_shadow ? shadow : nullptr);
         if (r) return r;
         merges16 += c->merge16_last;
+        const bool init_shadow = via_shadow && c->merge16_last;
         CUDA_TRY(cudaEventRecord(E[ev++], st));  // merge end of level m
         CUDA_TRY(cudaMemcpyAsync(h_max + m, d_max + m, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaEventRecord(c->evmax[m], st));
-        // Every merged value of level m is at most M(m-1) + M(1): the split
-        // {X \ t, t} bounds it, and relaxed values never exceed merged ones.
-        // 16-bit records when that bound is at most 32767.
-        bool u16 = false;
-        if (c->value_bits == 0) {
+        if (c->value_bits == 0 && m == 2) {
             CUDA_TRY(cudaEventSynchronize(c->evmax[m - 1]));
             u16 = (uint64_t)h_max[m - 1] + h_max[1] <= 32767;
         }
@@ -507,7 +515,7 @@ int run_dp(emv_ctx *c, int32_t n, const int32_t *row_ptr, const int2 *adj, int32
         for (int64_t off = 0; off < cnt; off += chunk) {
             const int32_t rows = (int32_t)std::min<int64_t>(chunk, cnt - off);
             r = launch_relax(c, row_ptr, adj, n, ld, table, xs + b + off, rows, d_terms, 0, st, u16, nullptr, shadow,
-                             sld);
+                             sld, init_shadow);
             if (r) return r;
             relax_launches++;
         }
