@@ -491,10 +491,8 @@ int run_dp(emv_ctx *c, int32_t n, const int32_t *row_ptr, const int2 *adj, int32
         bool m16 = false, u16 = false;
         if (c->value_bits == 0 && m >= 3) {
             CUDA_TRY(cudaEventSynchronize(c->evmax[m - 1]));
-            uint64_t worst = 0;
-            for (int32_t j = 1; 2 * j <= m; j++) worst = std::max<uint64_t>(worst, (uint64_t)h_max[j] + h_max[m - j]);
-            m16 = worst <= 65533;
-            u16 = (uint64_t)h_max[m - 1] + h_max[1] <= 32767;
+            m16 = merge16_allowed(h_max, m);
+            u16 = relax16_allowed(h_max, m);
         }
         // A level merged and relaxed in 16 bits keeps its merged rows only in
         // the shadow: the relaxation reads them there and writes the int32 rows.
@@ -508,7 +506,7 @@ int run_dp(emv_ctx *c, int32_t n, const int32_t *row_ptr, const int2 *adj, int32
         CUDA_TRY(cudaEventRecord(c->evmax[m], st));
         if (c->value_bits == 0 && m == 2) {
             CUDA_TRY(cudaEventSynchronize(c->evmax[m - 1]));
-            u16 = (uint64_t)h_max[m - 1] + h_max[1] <= 32767;
+            u16 = relax16_allowed(h_max, m);
         }
         levels16 += u16;
         const int32_t chunk = relax_chunk_rows_level(c, n, u16, cnt);

@@ -18,6 +18,15 @@ void subset_levels(int32_t k, std::vector<uint32_t> &xs, std::vector<int64_t> &o
 
 namespace emv {
 
+bool merge16_allowed(const uint32_t *M, int32_t m)
+{
+    uint64_t worst = 0;
+    for (int32_t j = 1; 2 * j <= m; j++) worst = std::max<uint64_t>(worst, (uint64_t)M[j] + M[m - j]);
+    return m >= 2 && worst <= 65533;
+}
+
+bool relax16_allowed(const uint32_t *M, int32_t m) { return m >= 2 && (uint64_t)M[m - 1] + M[1] <= 32767; }
+
 int32_t relax_rows_per_chunk(int64_t n, int64_t l2_bytes, bool u16)
 {
     // 256 int32 words a vertex is the relaxation scratch's capacity (CHUNK_ROWS)

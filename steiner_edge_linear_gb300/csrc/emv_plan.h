@@ -14,6 +14,15 @@ void subset_levels(int32_t k, std::vector<uint32_t> &xs, std::vector<int64_t> &o
 
 namespace emv {
 
+// Value widths of level m from the level maxima M[1..m-1] (M[j] = the largest
+// value level j's merge wrote, level 1: its relaxation; all ones = unknown).
+// 16-bit merge staging when every M[j] + M[m-j] <= 65533, so that no sum of
+// two staged values leaves 16 bits and a pad pair (>= 0xfffe) never wins;
+// 16-bit relaxation records when M[m-1] + M[1] <= 32767, which bounds every
+// merged, hence every relaxed, value of level m (split {X \ t, t}).
+bool merge16_allowed(const uint32_t *M, int32_t m);
+bool relax16_allowed(const uint32_t *M, int32_t m);
+
 // Rows per relaxation chunk of an n-vertex graph: 512-byte vertex records
 // while they fit in three quarters of L2 (the sweeps' gathers are then L2
 // hits and larger records only add bytes per sweep), else 1 KB ones, which

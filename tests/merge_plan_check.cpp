@@ -56,9 +56,40 @@ static int check_chunks()
     return ok ? 0 : 1;
 }
 
+// The value-width rules at their edges: exact thresholds, unknown maxima
+// (all ones) and sums that would overflow 32 bits.
+static int check_widths()
+{
+    bool ok = true;
+    auto want = [&](bool got, bool exp, const char *what) {
+        if (got != exp) {
+            std::printf("FAIL widths: %s\n", what);
+            ok = false;
+        }
+    };
+    uint32_t M[8] = {0, 16000, 16767, 30000, 0, 0, 0, 0};
+    want(relax16_allowed(M, 2), true, "2 * 16000 <= 32767");
+    want(relax16_allowed(M, 3), true, "16767 + 16000 = 32767");
+    M[2] = 16768;
+    want(relax16_allowed(M, 3), false, "16768 + 16000 > 32767");
+    want(merge16_allowed(M, 3), true, "16000 + 16768 <= 65533");
+    M[3] = 49533;
+    want(merge16_allowed(M, 4), true, "max(16000 + 49533, 2 * 16768) = 65533");
+    M[3] = 49534;
+    want(merge16_allowed(M, 4), false, "16000 + 49534 = 65534");
+    M[3] = 0xffffffffu;  // level 3 not recorded
+    want(merge16_allowed(M, 4), false, "unknown maximum");
+    want(relax16_allowed(M, 4), false, "unknown maximum, no 32-bit wrap");
+    M[1] = 0x80000000u;
+    want(relax16_allowed(M, 2), false, "2^31 + 2^31 must not wrap to 0");
+    if (ok) std::printf("ok widths\n");
+    return ok ? 0 : 1;
+}
+
 int main(int argc, char **argv)
 {
     if (argc == 2 && std::string(argv[1]) == "chunks") return check_chunks();
+    if (argc == 2 && std::string(argv[1]) == "widths") return check_widths();
     if (argc < 3) return 2;
     const int k = std::atoi(argv[1]);
     const int64_t smem = std::atoll(argv[2]);

@@ -39,6 +39,13 @@ def test_relaxation_chunk_rule(checker):
     assert out.returncode == 0 and out.stdout.startswith("ok chunks"), out.stdout + out.stderr
 
 
+def test_value_width_rules(checker):
+    """16-bit merge / relaxation rules at their thresholds, with unknown level
+    maxima and without 32-bit wrap-around."""
+    out = subprocess.run([checker, "widths"], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0 and out.stdout.startswith("ok widths"), out.stdout + out.stderr
+
+
 def test_smaller_budget_still_covers(checker):
     """A quarter of the shared memory forces more groups and row tiles."""
     out = subprocess.run([checker, "12", str(STREAM_SMEM_BYTES // 4)], capture_output=True, text=True, timeout=600)
