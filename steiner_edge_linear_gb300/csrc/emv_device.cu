@@ -155,8 +155,7 @@ static int grid_for(int64_t work, int threads, int cap)
 // value written.
 int launch_relax(emv_ctx *c, const int32_t *row_ptr, const int2 *adj, int32_t n, int64_t ld, int32_t *table,
                  const uint32_t *rows, int32_t nrows, const int32_t *terms, int32_t level1, cudaStream_t st,
-                 bool u16 = false, uint32_t *vmax = nullptr, uint16_t *shadow = nullptr, int64_t shadow_ld = 0,
-                 bool init_shadow = false)
+                 bool u16 = false, uint32_t *vmax = nullptr, uint16_t *shadow = nullptr, int64_t shadow_ld = 0)
 {
     RelaxArgs a;
     a.stamp = (int32_t *)c->stamp.ptr;
@@ -183,7 +182,6 @@ int launch_relax(emv_ctx *c, const int32_t *row_ptr, const int2 *adj, int32_t n,
     a.vmax = vmax;
     a.shadow = shadow;
     a.shadow_ld = shadow_ld;
-    a.init_shadow = init_shadow && u16 && shadow;
     const int32_t words = u16 ? (nrows + 1) / 2 : nrows;  // int32 words a vertex record needs
     // Without stamps a sweep pulls every arc, also from heads that did not
     // change: worth it once most heads changed while the records are L2 hits
@@ -369,8 +367,7 @@ static cudaError_t merge_smem_launch(emv_ctx *c, int32_t *table, int64_t ld, int
 // Merge of level m: the shared-memory kernel with the widest vertex block
 // whose staging fits, else the direct kernel (k above MERGE_SMEM_KMAX).
 int launch_merge(emv_ctx *c, int32_t *table, int64_t ld, int32_t n, int32_t k, int32_t m, const int32_t *d_terms,
-                 cudaStream_t st, bool u16 = false, const uint16_t *shadow = nullptr, int64_t shadow_ld = 0,
-                 uint16_t *shadow_out = nullptr)
+                 cudaStream_t st, bool u16 = false, const uint16_t *shadow = nullptr, int64_t shadow_ld = 0)
 {
     if (!c->merge_attr) {
         const void *fns[6] = {(const void *)k_merge_smem<32>, (const void *)k_merge_smem<16>,
@@ -402,7 +399,7 @@ int launch_merge(emv_ctx *c, int32_t *table, int64_t ld, int32_t n, int32_t k, i
             if (u16)
                 k_merge_stream16<<<(unsigned)((n + 63) / 64), 1024, (size_t)g.smem, st>>>(
                     table, ld, n, xg, (int32_t)g.cnt, pg, (int32_t)g.nphase, d_terms, k, (uint32_t *)c->lvlmax.ptr + m,
-                    shadow, shadow_ld, shadow_out);
+                    shadow, shadow_ld);
             else
                 k_merge_stream<<<(unsigned)((n + 31) / 32), 1024, (size_t)g.smem, st>>>(
                     table, ld, n, xg, (int32_t)g.cnt, pg, (int32_t)g.nphase, d_terms, k, (uint32_t *)c->lvlmax.ptr + m);
@@ -494,13 +491,9 @@ int run_dp(emv_ctx *c, int32_t n, const int32_t *row_ptr, const int2 *adj, int32
             m16 = merge16_allowed(h_max, m);
             u16 = relax16_allowed(h_max, m);
         }
-        // A level merged and relaxed in 16 bits keeps its merged rows only in
-        // the shadow: the relaxation reads them there and writes the int32 rows.
-        const bool via_shadow = m16 && u16 && shadow;
-        r = launch_merge(c, table, ld, n, k, m, d_terms, st, m16, shadow, sld, via_shadow ? shadow : nullptr);
+        r = launch_merge(c, table, ld, n, k, m, d_terms, st, m16, shadow, sld);
         if (r) return r;
         merges16 += c->merge16_last;
-        const bool init_shadow = via_shadow && c->merge16_last;
         CUDA_TRY(cudaEventRecord(E[ev++], st));  // merge end of level m
         CUDA_TRY(cudaMemcpyAsync(h_max + m, d_max + m, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
         CUDA_TRY(cudaEventRecord(c->evmax[m], st));
@@ -513,7 +506,7 @@ int run_dp(emv_ctx *c, int32_t n, const int32_t *row_ptr, const int2 *adj, int32
         for (int64_t off = 0; off < cnt; off += chunk) {
             const int32_t rows = (int32_t)std::min<int64_t>(chunk, cnt - off);
             r = launch_relax(c, row_ptr, adj, n, ld, table, xs + b + off, rows, d_terms, 0, st, u16, nullptr, shadow,
-                             sld, init_shadow);
+                             sld);
             if (r) return r;
             relax_launches++;
         }

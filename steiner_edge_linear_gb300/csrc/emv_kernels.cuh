@@ -46,7 +46,6 @@ struct RelaxArgs {
     uint32_t *vmax;         // if set: atomicMax of every value phase C writes
     uint16_t *shadow;       // if set: phase C also writes min(value, 0xffff) to shadow[X * shadow_ld + v]
     int64_t shadow_ld;
-    int32_t init_shadow;    // phase A reads the rows from the shadow (the 16-bit merge left them only there)
 };
 
 __global__ void k_fill(int32_t *__restrict__ p, int64_t count, int32_t value)
@@ -347,8 +346,7 @@ __global__ void __launch_bounds__(1024) k_merge_stream16(int32_t *__restrict__ t
                                                          const MergePhase *__restrict__ phases, int32_t nphase,
                                                          const int32_t *__restrict__ terms, int32_t k,
                                                          uint32_t *__restrict__ level_max,
-                                                         const uint16_t *__restrict__ shadow, int64_t sld,
-                                                         uint16_t *__restrict__ shadow_out)
+                                                         const uint16_t *__restrict__ shadow, int64_t sld)
 {
     extern __shared__ __align__(16) uint32_t sm[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -471,16 +469,14 @@ __global__ void __launch_bounds__(1024) k_merge_stream16(int32_t *__restrict__ t
                     if (tv == va) a0 = (uint32_t)table[(int64_t)(X ^ (1u << t)) * ld + va];
                     if (tv == va + 1) a1 = (uint32_t)table[(int64_t)(X ^ (1u << t)) * ld + va + 1];
                 }
-            if (shadow_out) {  // the level's 16-bit relaxation reads its rows from the shadow
-                uint16_t *dst = shadow_out + (int64_t)X * sld + va;
-                if (va + 1 < n) *reinterpret_cast<uint32_t *>(dst) = (a0 & 0xffffu) | a1 << 16;
-                else *dst = (uint16_t)a0;
+            int32_t *dst = table + (int64_t)X * ld + va;
+            if (va + 1 < n) {
+                *reinterpret_cast<int2 *>(dst) = make_int2((int32_t)a0, (int32_t)a1);
+                vmax = max(vmax, max(a0, a1));
             } else {
-                int32_t *dst = table + (int64_t)X * ld + va;
-                if (va + 1 < n) *reinterpret_cast<int2 *>(dst) = make_int2((int32_t)a0, (int32_t)a1);
-                else *dst = (int32_t)a0;
+                *dst = (int32_t)a0;
+                vmax = max(vmax, a0);
             }
-            vmax = max(vmax, va + 1 < n ? max(a0, a1) : a0);
         }
     vmax = __reduce_max_sync(FULL, vmax);
     if (lane == 0) atomicMax(&s_max, vmax);
@@ -663,7 +659,6 @@ __device__ __forceinline__ int32_t relax_load_value(const RelaxArgs &a, int32_t 
 {
     if (row >= a.nrows || v >= a.n) return U16 ? 0 : INF;
     if (a.level1) return (v == __ldg(a.terms + row)) ? 0 : INF;
-    if (U16 && a.init_shadow) return (int32_t)__ldcg(a.shadow + (int64_t)__ldg(a.rows + row) * a.shadow_ld + v);
     return __ldcg(a.table + (int64_t)__ldg(a.rows + row) * a.ld + v);
 }
 
