@@ -14,10 +14,15 @@ relaxations, cost read) with the CSR already resident in HBM; the working set
   roofline  the dominant kernel against the measured HBM copy bandwidth
   cpu_baseline  the reference's own emv_kernel (oracle/_ref) on the box's
          host cores, on a bounded sample of the same workload
+  batched, serve  the benchmark spec's two systems patterns measured in the same
+         run: 4096 mixed instances in one persistent launch, and a Poisson
+         request stream through the continuous-batching server, each against
+         plain one-instance-at-a-time GPU solves (--no-extras leaves them out)
 
-Other workloads: --workload batched (4096 mixed instances in one persistent
-launch vs one-at-a-time solves) and --workload serve (Poisson request
-stream, p50/p99 latency).  --impl reference times the reference instead.
+Other workloads alone: --workload batched, --workload serve, --workload
+roofline (n = 2^20, k = 14).  --impl reference times the reference instead
+(its process never loads the solver's library: the instance comes from the
+stand-alone generator executable).
 Multi-GPU (torchrun): independent replicas, one per rank.
 """
 from __future__ import annotations
@@ -50,6 +55,7 @@ def parse_args():
     p.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     p.add_argument("--workload", choices=["single", "roofline", "batched", "serve"], default="single")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-extras", action="store_true", help="single workload without the batched/serve sub-objects")
     p.add_argument("--batch-count", type=int, default=4096)
     p.add_argument("--serve-rates", type=str, default="2000,8000")
     p.add_argument("--serve-requests", type=int, default=4000)
@@ -178,36 +184,87 @@ def relax_bytes_per_row(n: int, m: int) -> float:
     return 12.0 * n + 16.0 * m + 4.0 * (n + 1)
 
 
+GEN_PATH = os.path.join(ROOT, "steiner_edge_linear_gb300", "lib", "emv-gen")
+
+
+def write_instance(path: str, *args) -> None:
+    """Writes a generated instance as STP with the stand-alone generator
+    executable (the same generator as the library, without loading the
+    library), e.g. write_instance(p, "regular", n, d, wmin, wmax, k, seed)."""
+    if not os.path.exists(GEN_PATH):
+        from steiner_edge_linear_gb300 import build as _b  # compiles only; loads nothing
+        _b.build()
+    subprocess.run([GEN_PATH] + [str(a) for a in args] + [path], check=True, stdout=subprocess.DEVNULL)
+
+
+def _single_args(cfg: dict) -> list:
+    return ["regular", cfg["n"], cfg["degree"], cfg["wmin"], cfg["wmax"], cfg["k"], cfg["seed"]]
+
+
 def cpu_reference_runs(steps: int, warmup: int, threads: int | None = None) -> dict:
     """Times complete solves of the benchmark instance with the reference's own
     emv_kernel (oracle/_ref, built from the reference source with -O3 and
     OpenMP) on the host cores; falls back to the oracle's C restatement where
-    the reference leg is not built.  Warm-up runs use the first 8 terminals."""
+    the reference leg is not built.  Warm-up runs use the first 8 terminals.
+    Nothing here loads the solver's library: the instance comes from the
+    stand-alone generator."""
     import oracle
-    import steiner_edge_linear_gb300 as E
 
     oracle.build(reference=True)
-    inst = E.StpInstance.regular(**SINGLE)
     threads = threads or os.cpu_count() or 1
-    runs = []
+    runs, cost = [], None
     with tempfile.TemporaryDirectory() as tmp:
         path = os.path.join(tmp, "single.stp")
-        inst.write(path)
+        write_instance(path, *_single_args(SINGLE))
         kind = "reference" if oracle.reference_available() else "port"
-        csr = E.Csr.from_stp(inst)
+        csr = None if kind == "reference" else oracle.read_stp_csr(path)
         for i in range(warmup + steps):
             kp = 8 if i < warmup else 0
             if kind == "reference":
                 r = oracle.ref_emv(path, kprefix=kp, threads=threads)
                 t = (r["zero_ms"] + r["kernel_ms"]) / 1000.0
+                c = r["cost"]
             else:
+                n, row, col, w, terms = csr
                 t0 = time.perf_counter()
-                terms = csr.terminals[:kp] if kp else csr.terminals
-                oracle.emv_table(csr.n, csr.row_ptr, csr.col, csr.w, terms, threads=threads)
+                _, c = oracle.emv_table(n, row, col, w, terms[:kp] if kp else terms, threads=threads)
                 t = time.perf_counter() - t0
             if i >= warmup:
                 runs.append(t)
-    return {"kind": kind, "threads": threads, "runs_s": runs}
+                cost = c
+    return {"kind": kind, "threads": threads, "runs_s": runs, "cost": cost}
+
+
+def reference_throughput(indices, base_seed: int) -> dict:
+    """The reference's emv_kernel (oracle/_ref) in throughput mode: one
+    single-threaded process per host core over a sample of the batched
+    distribution (instances written by the stand-alone generator)."""
+    import oracle
+    from concurrent.futures import ThreadPoolExecutor
+
+    oracle.build(reference=True)
+    cores = os.cpu_count() or 1
+    with tempfile.TemporaryDirectory() as tmp:
+        paths = []
+        for i in indices:
+            p = os.path.join(tmp, f"i{i}.stp")
+            write_instance(p, "mixed", base_seed, i)
+            paths.append(p)
+        kind = "reference" if oracle.reference_available() else "port"
+
+        def one(p):
+            if kind == "reference":
+                oracle.ref_emv(p, threads=1)
+            else:
+                n, row, col, w, terms = oracle.read_stp_csr(p)
+                oracle.emv_table(n, row, col, w, terms, threads=1)
+
+        t0 = time.perf_counter()
+        with ThreadPoolExecutor(max_workers=cores) as ex:
+            done = sum(1 for _ in ex.map(one, paths))
+        wall = time.perf_counter() - t0
+    return {"value": round(done / wall, 2), "unit": "solves/s", "cores": cores, "kind": kind,
+            "sample": f"{done} instances of the same distribution, one single-threaded process per core"}
 
 
 def run_single(args, dist: Dist, cfg: dict = SINGLE, cfg_name: str = SINGLE_NAME) -> dict:
@@ -253,19 +310,23 @@ def run_single(args, dist: Dist, cfg: dict = SINGLE, cfg_name: str = SINGLE_NAME
     ms = dist.max(ms)
     value = args.steps * dist.world / (ms / 1000.0)
 
-    # e2e through emv_solve with pinned host CSR: H2D of the graph + D2H of the cost per step
+    # e2e through emv_solve with pinned host CSR: H2D of the graph + D2H of the cost per step;
+    # the default call (admission checks on), and the same call without the host-side checks
     pin = [torch.from_numpy(a).pin_memory() for a in (csr.row_ptr, csr.col, csr.w)]
     hcsr = E.Csr(n, pin[0].numpy(), pin[1].numpy(), pin[2].numpy(), csr.terminals)
-    for _ in range(2):
-        solver.solve(hcsr, check=False, stream=sp)
-    dist.barrier()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        r = solver.solve(hcsr, check=False, stream=sp)
-        assert r.cost == cost
-    torch.cuda.synchronize()
-    e2e_s = dist.max(time.perf_counter() - t0)
+    e2e = {}
+    for check in (True, False):
+        for _ in range(2):
+            solver.solve(hcsr, check=check, stream=sp)
+        dist.barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            r = solver.solve(hcsr, check=check, stream=sp)
+            assert r.cost == cost
+        torch.cuda.synchronize()
+        e2e[check] = dist.max(time.perf_counter() - t0)
+    e2e_s = e2e[True]
     h2d = 4 * (n + 1) + 8 * csr.arcs + 4 * k
     d2h = 4 + 16
 
@@ -303,7 +364,9 @@ def run_single(args, dist: Dist, cfg: dict = SINGLE, cfg_name: str = SINGLE_NAME
            "config": single_config(cfg, cfg_name, dist.world),
            "cost": cost,
            "e2e": {"value": round(args.steps * dist.world / e2e_s, 4), "unit": "solves/s",
-                   "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                   "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                   "call": "emv_solve, default flags (host admission checks on)",
+                   "without_host_checks": round(args.steps * dist.world / e2e[False], 4)},
            "gpu_launches": launches * args.steps,
            "phases_ms": {"merge": round(merge_ms, 3), "relax_incl_level1": round(relax_ms, 3),
                          "kernel": round(kernel_ms, 3)},
@@ -320,9 +383,34 @@ def run_single(args, dist: Dist, cfg: dict = SINGLE, cfg_name: str = SINGLE_NAME
         c = cpu_reference_runs(steps=1, warmup=0)
         t = statistics.median(c["runs_s"])
         out["cpu_baseline"] = {"value": round(1.0 / t, 5), "unit": "solves/s", "cores": c["threads"],
-                               "kind": c["kind"],
+                               "kind": c["kind"], "cost": c["cost"],
                                "sample": (f"one complete solve of the same instance (all 4096 rows, {t:.2f} s) by the "
                                           f"reference's emv_kernel, -O3, {c['threads']} OpenMP threads")}
+    return out
+
+
+def extras(args, dist) -> dict:
+    """The batched and serving workloads of the default line, each with its
+    own clocks: the benchmark spec's batched/served solves/s against plain
+    one-instance-at-a-time GPU solves (config: 4096 mixed instances; a
+    Poisson stream at one saturating arrival rate)."""
+    from steiner_edge_linear_gb300 import benchmarks
+
+    out = {}
+    b = benchmarks.run_batched(args, dist, clock=lambda: ClockSampler(dist.local))
+    out["batched"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "e2e", "plain_gpu_one_at_a_time",
+                                        "batched_vs_plain", "clocks")}
+    out["batched"]["workload"] = b["config"]["workload"]
+    out["batched"]["autotuned"] = {k: b["config"][k] for k in b["config"] if k != "workload"}
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        out["batched"]["cpu_baseline"] = reference_throughput(range(0, 256), benchmarks.MIXED_BASE)
+    one_rate = argparse.Namespace(**vars(args))
+    one_rate.serve_rates = args.serve_rates.split(",")[-1]  # the saturating rate only
+    sv = benchmarks.run_serve(one_rate, dist, clock=lambda: ClockSampler(dist.local))
+    if sv is not None:
+        out["serve"] = {k: sv[k] for k in ("value", "unit", "rates", "plain_gpu_sequential", "served_vs_plain",
+                                           "clocks")}
+        out["serve"]["workload"] = sv["config"]["workload"]
     return out
 
 
@@ -344,6 +432,7 @@ def run_reference(args, dist: Dist) -> dict | None:
     t = statistics.median(c["runs_s"])
     value = 1.0 / t
     return {"metric": "solves/s", "value": round(value, 5), "unit": "solves/s", "n_gpus": dist.world,
+            "cost": c["cost"],
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000.0 * t, 1), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int64",
             "data": "synthetic (seeded generator, configuration-model random regular graph)",
@@ -362,14 +451,20 @@ def main():
             out = run_reference(args, dist)
         elif args.workload == "single":
             out = run_single(args, dist)
+            if not args.no_extras:
+                ex = extras(args, dist)
+                if out is not None:
+                    out.update(ex)
         elif args.workload == "roofline":
             out = run_single(args, dist, ROOFLINE, ROOFLINE_NAME)
         elif args.workload == "batched":
             from steiner_edge_linear_gb300 import benchmarks
-            out = benchmarks.run_batched(args, dist)
+            out = benchmarks.run_batched(args, dist, clock=lambda: ClockSampler(dist.local))
+            if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+                out["cpu_baseline"] = reference_throughput(range(0, 256), benchmarks.MIXED_BASE)
         else:
             from steiner_edge_linear_gb300 import benchmarks
-            out = benchmarks.run_serve(args, dist)
+            out = benchmarks.run_serve(args, dist, clock=lambda: ClockSampler(dist.local))
         if out is not None and dist.rank == 0:
             print(json.dumps(out), flush=True)
     finally:

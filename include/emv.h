@@ -201,8 +201,11 @@ typedef struct emv_timing {
  * on device-resident data: d_row_ptr/d_col/d_w are a device CSR, d_table a
  * caller-owned device table of (1<<k) rows of stride ld >= n (ld a multiple
  * of 4) that this call fills completely, terminals a host array of k ids.
- * *cost_out receives d[C][q].  Asynchronous on stream except for the scalar
- * cost read and the relaxation's convergence flag. */
+ * *cost_out receives d[C][q].  Admission checks as emv_solve's (always on):
+ * the device CSR is checked before the DP reads it (EMV_ERR_BAD_INPUT,
+ * EMV_ERR_OVERFLOW) and a graph the level-1 closures do not span is
+ * EMV_ERR_DISCONNECTED.  Asynchronous on stream except for the check's and
+ * the level maxima's scalar reads and the final cost read. */
 int emv_kernel_dev(emv_ctx *ctx, int32_t n, int64_t arcs,
                    const int32_t *d_row_ptr, const int32_t *d_col,
                    const int32_t *d_w, int32_t k, const int32_t *terminals,
@@ -212,7 +215,7 @@ int emv_kernel_dev(emv_ctx *ctx, int32_t n, int64_t arcs,
 /* Flags of emv_solve. */
 #define EMV_SOLVE_TREE  0x1   /* recover a tree (R:2301-2310, -list)        */
 #define EMV_SOLVE_TABLE 0x2   /* copy the table to out->table               */
-#define EMV_SOLVE_NOCHECK 0x4 /* skip the host connectivity/overflow check  */
+#define EMV_SOLVE_NOCHECK 0x4 /* skip the admission checks (below)          */
 
 typedef struct emv_result {
     int64_t cost;          /* d[C][q], INT64_MAX when unreachable / k == 1 */
@@ -227,11 +230,20 @@ typedef struct emv_result {
 /* Mirrors erickson_monma_veinott(root, list_soln) (R:2141-2343): host CSR and
  * terminals in, cost (and optional tree and table) out.  Copies the graph to
  * the device, allocates the table from the context, runs the DP, optionally
- * recovers a tree of real graph edges whose weight equals the cost. */
+ * recovers a tree of real graph edges whose weight equals the cost.
+ * Admission checks (unless EMV_SOLVE_NOCHECK), the same statuses as
+ * emv_graph_check: before any DP kernel reads the graph, one device pass
+ * checks row_ptr (0 .. arcs, non-decreasing), every head (0 <= v < n) and
+ * weight (0 <= w < 2^30) and bounds every finite table value by
+ * min((n-1) * max_w, sum of edge weights), rejecting EMV_ERR_BAD_INPUT /
+ * EMV_ERR_OVERFLOW; a graph that is not connected (a vertex the level-1
+ * closures leave unreached) is EMV_ERR_DISCONNECTED after the DP.  The CSR
+ * must hold both arcs of every edge. */
 int emv_solve(emv_ctx *ctx, const emv_graph *g, const int32_t *terminals,
               int32_t k, int32_t flags, emv_result *out, void *stream);
 
-/* Same as emv_solve with a device-resident CSR (no graph copy). */
+/* Same as emv_solve with a device-resident CSR (no graph copy), with the
+ * same admission checks on the device. */
 int emv_solve_dev(emv_ctx *ctx, const emv_graph *d_g, const int32_t *terminals,
                   int32_t k, int32_t flags, emv_result *out, void *stream);
 
@@ -247,15 +259,24 @@ int emv_sssp(emv_ctx *ctx, const emv_graph *g, int32_t source,
  * synchronisation, or a host application forbids allocation after start-up):
  * for r < rows, d_out[r*ld + v] = min over u of d_init[r*ld + u] + dist(u, v)
  * on the device CSR (d_row_ptr, d_col, d_w), EMV_INF32 meaning "no value".
+ * Input conditions: the CSR holds both arcs of every edge (a changed vertex
+ * wakes only the heads of its own arcs), row_ptr runs from 0 to arcs without
+ * decreasing, heads are in [0, n), weights in [0, 2^30), and every d_init
+ * value is at most EMV_INF32.  The CSR is checked on the device before the
+ * closure reads it (EMV_ERR_BAD_INPUT; a weight of 2^30 or more is
+ * EMV_ERR_OVERFLOW), an init value above EMV_INF32 is EMV_ERR_BAD_INPUT, and
+ * a finite result that would reach EMV_INF32 is EMV_ERR_OVERFLOW (sums
+ * saturate at EMV_INF32, they never wrap).
  * Its working memory is one fixed device array of about 17 MiB inside the
  * library, held on every GPU that loads the library until the process exits;
  * limits: n <= 131072 vertices and rows <= 32 (larger sizes return
  * EMV_ERR_BAD_INPUT).  It calls no allocator.  The first call on a device
  * looks up that array's device address (set-up, done once per device with
- * the device current); make that first call before any stream capture.
- * Every call shares the array, so calls whose executions overlap on the GPU
- * race: issue them on one stream or otherwise serialise them.  d_out may
- * equal d_init.  Waits for the stream to read the completion status. */
+ * the device current).  The call waits on the stream for its check and its
+ * status, so it cannot be captured into a CUDA graph: on a capturing stream
+ * it returns EMV_ERR_BAD_INPUT without touching the stream.  Every call
+ * shares the array, so calls whose executions overlap on the GPU race: issue
+ * them on one stream or otherwise serialise them.  d_out may equal d_init. */
 int emv_closure_noalloc(int32_t n, int64_t arcs, const int32_t *d_row_ptr,
                         const int32_t *d_col, const int32_t *d_w,
                         const int32_t *d_init, int32_t rows, int64_t ld,
@@ -284,6 +305,15 @@ typedef struct emv_batch_stats {
  * gets one int64 per instance. */
 int emv_batch_solve(emv_ctx *ctx, const emv_instance *inst, int32_t count,
                     int64_t *costs_out, emv_batch_stats *stats, void *stream);
+
+/* emv_batch_solve that also returns every instance's finished DP table:
+ * tables_out[i] (a host buffer of (1 << k_i) * n_i int32, FV_INDEX order
+ * X * n_i + v like R:691; NULL skips instance i) receives the table the
+ * batched launch wrote, the same cells the reference's write-back defines
+ * (R:2117-2130).  No counterpart in the reference. */
+int emv_batch_solve_tables(emv_ctx *ctx, const emv_instance *inst, int32_t count,
+                           int64_t *costs_out, int32_t *const *tables_out,
+                           emv_batch_stats *stats, void *stream);
 
 /* Autotuner of the batched launch (no counterpart in the reference): for
  * every instance class present in inst (n bucket <=256, <=1024, <=4096,

@@ -26,7 +26,10 @@ REF_DIR = os.path.join(ORACLE_DIR, "_ref")
 REF_EMV = os.path.join(REF_DIR, "ref_emv")
 REF_EMV_OPT = os.path.join(REF_DIR, "ref_emv_opt")
 REF_READER = os.path.join(REF_DIR, "reader-el")
+# the reference's shipped test instances, staged by the recipe (Makefile "stage")
+TESTSET_DIR = os.path.join(REF_DIR, "testset")
 INF32 = 1 << 30
+FNV_BASIS = 1469598103934665603
 
 _lib = None
 
@@ -59,6 +62,8 @@ def _load():
         lib.oracle_sssp.argtypes = [ctypes.c_int32, P, P, P, ctypes.c_int32, P]
         lib.oracle_fnv64.restype = ctypes.c_uint64
         lib.oracle_fnv64.argtypes = [P, ctypes.c_int64]
+        lib.oracle_fnv64_from.restype = ctypes.c_uint64
+        lib.oracle_fnv64_from.argtypes = [P, ctypes.c_int64, ctypes.c_uint64]
         _lib = lib
     return _lib
 
@@ -91,9 +96,71 @@ def sssp(n: int, row_ptr, col, w, source: int) -> np.ndarray:
     return d
 
 
-def fnv64(a: np.ndarray) -> int:
+def closure(n: int, row_ptr, col, w, init: np.ndarray) -> np.ndarray:
+    """Multi-source closure of each row of init (shape (rows, n), INF32 = no
+    value): out[r][v] = min over u of init[r][u] + dist(u, v), as int64 with
+    INF32 where nothing reaches v.  Each row is one Dijkstra (oracle_sssp)
+    from a virtual source whose arcs to u weigh init[r][u] -- the reference's
+    virtual-source relaxation (reader-el.c:2090-2116)."""
+    row_ptr = np.ascontiguousarray(row_ptr, dtype=np.int64)
+    col = np.ascontiguousarray(col, dtype=np.int64)
+    w = np.ascontiguousarray(w, dtype=np.int64)
+    arcs = int(row_ptr[n])
+    out = np.empty(init.shape, np.int64)
+    for r in range(init.shape[0]):
+        src = np.nonzero(init[r] < INF32)[0]
+        rp = np.concatenate([row_ptr, [arcs + src.size]]).astype(np.int32)
+        cc = np.concatenate([col[:arcs], src]).astype(np.int32)
+        ww = np.concatenate([w[:arcs], init[r][src].astype(np.int64)]).astype(np.int32)
+        d = sssp(n + 1, rp, cc, ww, n)[:n]
+        out[r] = np.where(d == np.iinfo(np.int64).max, INF32, d)
+    return out
+
+
+def fnv64(a: np.ndarray, h: int = FNV_BASIS) -> int:
+    """FNV-1a 64 of the int32 words' bytes; pass the previous result as h to
+    hash a table piece by piece (the reference harness hashes it whole)."""
     a = np.ascontiguousarray(a, dtype=np.int32)
-    return int(_load().oracle_fnv64(a.ctypes.data, a.size))
+    return int(_load().oracle_fnv64_from(a.ctypes.data, a.size, h))
+
+
+def read_stp_csr(path: str):
+    """(n, row_ptr, col, w, terminals) of an STP file, int32, 0-based, with
+    the arcs in the order root_build fills them (reader-el.c:794-826: edge
+    order, both arcs of every edge).  Reads only what the solver's own writer
+    emits ("e u v w" and "t v" lines), for CPU baselines that must not load
+    the solver's library."""
+    n = 0
+    edges, terms = [], []
+    with open(path) as f:
+        for line in f:
+            tok = line.split()
+            if not tok:
+                continue
+            if tok[0] == "nodes":
+                n = int(tok[1])
+            elif tok[0] == "e" and len(tok) >= 4:
+                edges.append((int(tok[1]) - 1, int(tok[2]) - 1, int(tok[3])))
+            elif tok[0] == "t" and len(tok) >= 2:
+                terms.append(int(tok[1]) - 1)
+    e = np.asarray(edges, dtype=np.int64).reshape(-1, 3)
+    src = np.stack([e[:, 0], e[:, 1]], axis=1).reshape(-1)
+    dst = np.stack([e[:, 1], e[:, 0]], axis=1).reshape(-1)
+    wt = np.repeat(e[:, 2], 2)
+    order = np.argsort(src, kind="stable")
+    row_ptr = np.zeros(n + 1, np.int32)
+    np.cumsum(np.bincount(src, minlength=n), out=row_ptr[1:])
+    return (n, row_ptr, dst[order].astype(np.int32), wt[order].astype(np.int32),
+            np.asarray(terms, dtype=np.int32))
+
+
+def testset_files() -> list:
+    """The reference's 204 SteinLib and 3 path instances (staged copies), or []."""
+    import glob
+
+    files = sorted(glob.glob(os.path.join(TESTSET_DIR, "small-instances", "*", "*.stp")))
+    files += sorted(glob.glob(os.path.join(TESTSET_DIR, "path", "*.stp")))
+    return files
 
 
 _REF_LINE = re.compile(r"^REF cost=(-?\d+) zero_ms=([\d.]+) kernel_ms=([\d.]+) n=(\d+) m=(\d+) k=(\d+) "

@@ -266,10 +266,11 @@ int oracle_emv(int32_t n, const int32_t *row_ptr, const int32_t *col,
     return overflow ? 3 : 0;
 }
 
-/* FNV-1a 64 over the bytes of int32 words (little-endian order of each word). */
-uint64_t oracle_fnv64(const int32_t *a, int64_t count)
+/* FNV-1a 64 over the bytes of int32 words (little-endian order of each word),
+ * continuing from the state h (the offset basis 1469598103934665603 starts a
+ * hash), so that a large table can be hashed in pieces. */
+uint64_t oracle_fnv64_from(const int32_t *a, int64_t count, uint64_t h)
 {
-    uint64_t h = 1469598103934665603ULL;
     for (int64_t i = 0; i < count; i++) {
         uint32_t x = (uint32_t)a[i];
         for (int b = 0; b < 4; b++) {
@@ -278,4 +279,9 @@ uint64_t oracle_fnv64(const int32_t *a, int64_t count)
         }
     }
     return h;
+}
+
+uint64_t oracle_fnv64(const int32_t *a, int64_t count)
+{
+    return oracle_fnv64_from(a, count, 1469598103934665603ULL);
 }

@@ -134,6 +134,8 @@ SIGNATURES = {
     "emv_sssp": (ctypes.c_int, [_P, ctypes.POINTER(_Graph), _I32, _P, ctypes.POINTER(ctypes.c_float), _P]),
     "emv_closure_noalloc": (ctypes.c_int, [_I32, _I64, _P, _P, _P, _P, _I32, _I64, _P, _P]),
     "emv_batch_solve": (ctypes.c_int, [_P, ctypes.POINTER(_Instance), _I32, _P, ctypes.POINTER(_BatchStats), _P]),
+    "emv_batch_solve_tables": (ctypes.c_int, [_P, ctypes.POINTER(_Instance), _I32, _P, _P,
+                                              ctypes.POINTER(_BatchStats), _P]),
     "emv_batch_autotune": (ctypes.c_int, [_P, ctypes.POINTER(_Instance), _I32, _P, _P]),
     "emv_batch_set_tuning": (ctypes.c_int, [_P, _P, _I32]),
     "emv_server_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.POINTER(_ServerOpts)]),
@@ -511,14 +513,22 @@ class Solver:
         """Shortest-path closure of up to 32 device rows with no device allocation (emv_closure_noalloc)."""
         _check(load_library().emv_closure_noalloc(n, arcs, row_ptr, col, w, init, rows, ld, out, stream))
 
-    def batch_solve(self, graphs: Sequence[Csr], stream: Optional[int] = None) -> tuple[np.ndarray, dict]:
-        """Many independent instances in one persistent launch (emv_batch_solve)."""
+    def batch_solve(self, graphs: Sequence[Csr], stream: Optional[int] = None, tables: bool = False):
+        """Many independent instances in one persistent launch (emv_batch_solve);
+        with tables=True also every instance's (2^k, n) table
+        (emv_batch_solve_tables) as a third return value."""
         count = len(graphs)
         insts, _keep = self._instances(graphs)
         costs = np.zeros(count, np.int64)
         st = _BatchStats()
-        _check(self._lib.emv_batch_solve(self._ctx, insts, count, costs.ctypes.data, ctypes.byref(st), stream))
-        return costs, {f: getattr(st, f) for f, _ in _BatchStats._fields_}
+        if not tables:
+            _check(self._lib.emv_batch_solve(self._ctx, insts, count, costs.ctypes.data, ctypes.byref(st), stream))
+            return costs, {f: getattr(st, f) for f, _ in _BatchStats._fields_}
+        tabs = [np.empty(((1 << g.k), g.n), np.int32) for g in graphs]
+        ptrs = (ctypes.c_void_p * max(count, 1))(*[t.ctypes.data for t in tabs])
+        _check(self._lib.emv_batch_solve_tables(self._ctx, insts, count, costs.ctypes.data, ptrs,
+                                                ctypes.byref(st), stream))
+        return costs, {f: getattr(st, f) for f, _ in _BatchStats._fields_}, tabs
 
 
 class Server:

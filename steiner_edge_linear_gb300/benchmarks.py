@@ -4,8 +4,7 @@ batched: 4096 independent instances of the mixed distribution (n log-uniform
   in [64, 4096], degree {3,4,6,8}, k uniform in [4, 10], weights [1, 1000],
   about 10% group instances; instance i is generated from seed base + i),
   solved by one persistent, graph-captured launch; compared with the plain
-  one-instance-at-a-time GPU solve and with the reference on the host cores
-  (one single-threaded process per core).
+  one-instance-at-a-time GPU solve.
 serve: Poisson arrivals of instances from the same distribution plus 2%
   large ones (n = 2^17, degree 8, k = 12), admitted by table footprint
   against a 150 GB budget; p50/p99 latency and solves/s per arrival rate,
@@ -13,15 +12,10 @@ serve: Poisson arrivals of instances from the same distribution plus 2%
 """
 from __future__ import annotations
 
-import os
+import contextlib
 import random
 import statistics
-import subprocess
-import sys
-import tempfile
-import threading
 import time
-from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 
@@ -50,42 +44,19 @@ def percentile(xs, q):
     return xs[i]
 
 
-def _reference_throughput(graphs_idx, seconds_budget: float = 20.0) -> dict:
-    """The reference's emv_kernel (oracle/_ref) in throughput mode: one
-    single-threaded process per host core over a sample of the instances."""
-    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
-    import oracle
-
-    oracle.build(reference=True)
-    cores = os.cpu_count() or 1
-    with tempfile.TemporaryDirectory() as tmp:
-        paths = []
-        for i in graphs_idx:
-            p = os.path.join(tmp, f"i{i}.stp")
-            StpInstance.mixed(MIXED_BASE, i).write(p)
-            paths.append(p)
-        kind = "reference" if oracle.reference_available() else "port"
-
-        def one(p):
-            t0 = time.perf_counter()
-            if kind == "reference":
-                oracle.ref_emv(p, threads=1)
-            else:
-                g = Csr.from_stp(StpInstance.from_file(p))
-                oracle.emv_table(g.n, g.row_ptr, g.col, g.w, g.terminals, threads=1)
-            return time.perf_counter() - t0
-
-        t0 = time.perf_counter()
-        done = 0
-        with ThreadPoolExecutor(max_workers=cores) as ex:
-            for _ in ex.map(one, paths):
-                done += 1
-        wall = time.perf_counter() - t0
-    return {"value": done / wall, "unit": "solves/s", "cores": cores, "kind": kind,
-            "sample": f"{done} instances of the same distribution, one single-threaded process per core"}
+class _NoClock:
+    def summary(self) -> dict:
+        return {}
 
 
-def run_batched(args, dist) -> dict:
+@contextlib.contextmanager
+def _no_clock():
+    yield _NoClock()
+
+
+def run_batched(args, dist, clock=_no_clock) -> dict:
+    """`clock()` is a context manager that samples the GPU clocks while the
+    timed steps run; its summary() goes into the line's "clocks"."""
     import torch
 
     dev = torch.device("cuda", dist.local)
@@ -99,12 +70,13 @@ def run_batched(args, dist) -> dict:
         costs, st = solver.batch_solve(graphs, stream=stream)
     dist.barrier()
     dev_ms, wall = [], []
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        c2, st = solver.batch_solve(graphs, stream=stream)
-        wall.append(time.perf_counter() - t0)
-        dev_ms.append(st["total_ms"])
-        assert np.array_equal(c2, costs)
+    with clock() as clk:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            c2, st = solver.batch_solve(graphs, stream=stream)
+            wall.append(time.perf_counter() - t0)
+            dev_ms.append(st["total_ms"])
+            assert np.array_equal(c2, costs)
     dist.barrier()
     ms = dist.max(statistics.median(dev_ms))
     e2e_s = dist.max(statistics.median(wall))
@@ -130,14 +102,14 @@ def run_batched(args, dist) -> dict:
                    "d2h_bytes_per_step": 8 * len(graphs) + 4},
            "plain_gpu_one_at_a_time": {"value": round(plain_rate, 1), "unit": "solves/s",
                                        "sample": f"first {len(sample)} instances, emv_solve each"},
-           "batched_vs_plain": round(count / (ms / 1000.0) / plain_rate, 1)}
-    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = _reference_throughput(range(0, 256))
+           "batched_vs_plain": round(count / (ms / 1000.0) / plain_rate, 1),
+           "clocks": clk.summary()}
     return out
 
 
-def run_serve(args, dist) -> dict | None:
-    """Poisson request stream against the continuous-batching server."""
+def run_serve(args, dist, clock=_no_clock) -> dict | None:
+    """Poisson request stream against the continuous-batching server; the
+    clocks are sampled while the requests are served."""
     import torch
 
     if dist.rank != 0:
@@ -164,31 +136,32 @@ def run_serve(args, dist) -> dict | None:
             s.solve(g, check=False)
         plain_rate = n_plain / (time.perf_counter() - t0)
     results = []
-    for rate in [float(x) for x in args.serve_rates.split(",")]:
-        with Server(dist.local, hbm_budget_bytes=150 * 10**9, max_slots=4096, large_n=65536) as srv:
-            ids = []
-            t_start = time.perf_counter()
-            next_t = t_start
-            for g in stream:
-                next_t += rng.expovariate(rate)
-                delay = next_t - time.perf_counter()
-                if delay > 0:
-                    time.sleep(delay)
-                ids.append(srv.submit(g))
-            lat = []
-            costs = []
-            for r in ids:
-                c, l_ms = srv.wait(r, 3600)
-                costs.append(c)
-                lat.append(l_ms)
-            wall = time.perf_counter() - t_start
-            st = srv.stats()
-        assert costs[:64] == want, "served costs differ from single solves"
-        small = [l for l, kd in zip(lat, kinds) if kd == "mixed"]
-        results.append({"arrival_rate": rate, "solves_per_s": round(len(ids) / wall, 1),
-                        "p50_ms": round(percentile(lat, 50), 3), "p99_ms": round(percentile(lat, 99), 3),
-                        "p99_small_ms": round(percentile(small, 99), 3), "waves": st["waves"],
-                        "peak_resident": st["peak_resident"], "peak_bytes": st["peak_bytes"]})
+    with clock() as clk:
+        for rate in [float(x) for x in args.serve_rates.split(",")]:
+            with Server(dist.local, hbm_budget_bytes=150 * 10**9, max_slots=4096, large_n=65536) as srv:
+                ids = []
+                t_start = time.perf_counter()
+                next_t = t_start
+                for g in stream:
+                    next_t += rng.expovariate(rate)
+                    delay = next_t - time.perf_counter()
+                    if delay > 0:
+                        time.sleep(delay)
+                    ids.append(srv.submit(g))
+                lat = []
+                costs = []
+                for r in ids:
+                    c, l_ms = srv.wait(r, 3600)
+                    costs.append(c)
+                    lat.append(l_ms)
+                wall = time.perf_counter() - t_start
+                st = srv.stats()
+            assert costs[:64] == want, "served costs differ from single solves"
+            small = [l for l, kd in zip(lat, kinds) if kd == "mixed"]
+            results.append({"arrival_rate": rate, "solves_per_s": round(len(ids) / wall, 1),
+                            "p50_ms": round(percentile(lat, 50), 3), "p99_ms": round(percentile(lat, 99), 3),
+                            "p99_small_ms": round(percentile(small, 99), 3), "waves": st["waves"],
+                            "peak_resident": st["peak_resident"], "peak_bytes": st["peak_bytes"]})
     best = max(r["solves_per_s"] for r in results)
     return {"metric": "solves/s", "value": best, "unit": "solves/s", "n_gpus": 1, "steps": len(results),
             "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
@@ -197,4 +170,5 @@ def run_serve(args, dist) -> dict | None:
             "rates": results,
             "plain_gpu_sequential": {"value": round(plain_rate, 1), "unit": "solves/s",
                                      "sample": f"first {n_plain} requests of the stream, emv_solve each"},
-            "served_vs_plain": round(best / plain_rate, 1)}
+            "served_vs_plain": round(best / plain_rate, 1),
+            "clocks": clk.summary()}

@@ -4,7 +4,10 @@ Products (under ``steiner_edge_linear_gb300/lib/``, git-ignored):
   * ``libemv.so``      -- the C-ABI library of ``include/emv.h``: host code
     (STP reader, CSR, generator, server) and the sm_103a CUDA kernels;
   * ``reader-el-gpu``  -- the command-line front end with the flags and output
-    lines of the reference's ``reader-el``.
+    lines of the reference's ``reader-el``;
+  * ``emv-gen``        -- the instance generator as a stand-alone executable
+    (host sources only, no CUDA, no libemv.so), for processes that must not
+    load the solver.
 
 Every CUDA translation unit is compiled for sm_103a only
 (``-gencode arch=compute_103a,code=sm_103a``).  Host code is compiled with
@@ -27,6 +30,7 @@ LIB_DIR = os.path.join(PKG_DIR, "lib")
 OBJ_DIR = os.path.join(LIB_DIR, "obj")
 LIB_PATH = os.path.join(LIB_DIR, "libemv.so")
 CLI_PATH = os.path.join(LIB_DIR, "reader-el-gpu")
+GEN_PATH = os.path.join(LIB_DIR, "emv-gen")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = [
@@ -39,6 +43,7 @@ SOURCES = [
     "emv_plan.cpp",
 ]
 CLI_SOURCES = ["cli.cpp"]
+GEN_SOURCES = ["gen_main.cpp", "emv_host.cpp"]
 
 
 def _nvcc() -> str:
@@ -73,7 +78,7 @@ def _run(cmd: list[str]) -> None:
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
-    """Compiles libemv.so and reader-el-gpu if any source changed; returns the library path."""
+    """Compiles libemv.so, reader-el-gpu and emv-gen if any source changed; returns the library path."""
     os.makedirs(OBJ_DIR, exist_ok=True)
     nvcc = _nvcc()
     headers = _headers()
@@ -95,8 +100,12 @@ def build(force: bool = False, verbose: bool = False) -> str:
         _run([nvcc] + ARCH + ["-shared", "-o", LIB_PATH] + objs + ["-lpthread"])
     cli_srcs = [os.path.join(CSRC, s) for s in CLI_SOURCES]
     if force or _stale(CLI_PATH, cli_srcs + headers + [LIB_PATH]):
-        _run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-Wall", "-I", INCLUDE, "-o", CLI_PATH]
+        _run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-Wall", "-I", INCLUDE, "-I", CSRC, "-o", CLI_PATH]
              + cli_srcs + ["-L", LIB_DIR, "-lemv", "-Wl,-rpath,$ORIGIN"])
+    gen_srcs = [os.path.join(CSRC, s) for s in GEN_SOURCES]
+    if force or _stale(GEN_PATH, gen_srcs + headers):
+        _run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-Wall", "-I", INCLUDE, "-I", CSRC, "-o", GEN_PATH]
+             + gen_srcs + ["-static-libstdc++", "-static-libgcc"])
     if verbose:
         print(f"built {LIB_PATH} ({len(jobs)} units recompiled)", file=sys.stderr)
     return LIB_PATH

@@ -139,8 +139,10 @@ double batch_work(int32_t n, int32_t k, int64_t arcs)
     return std::pow(3.0, k) * n * 0.5 + std::pow(2.0, k) * (double)arcs * 6.0;
 }
 
-extern "C" int emv_batch_solve(emv_ctx *c, const emv_instance *inst, int32_t count, int64_t *costs_out,
-                               emv_batch_stats *stats, void *stream)
+// emv_batch_solve and emv_batch_solve_tables: tables_out (or null) receives
+// the finished table of every instance whose entry is not null.
+static int batch_solve(emv_ctx *c, const emv_instance *inst, int32_t count, int64_t *costs_out,
+                       int32_t *const *tables_out, emv_batch_stats *stats, void *stream)
 {
     if (!c || (count > 0 && (!inst || !costs_out)) || count < 0)
         return emv_fail(EMV_ERR_BAD_INPUT, "emv_batch_solve: bad arguments");
@@ -190,6 +192,17 @@ extern "C" int emv_batch_solve(emv_ctx *c, const emv_instance *inst, int32_t cou
     CUDA_TRY(cudaMemcpyAsync(&err, a.err, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
     if (err) return emv_dev_status_to_emv(err);
+    if (tables_out) {
+        // instance order[j] ran in launch slot j; its table (ld = n) is at table_off[j]
+        for (int32_t j = 0; j < count; j++) {
+            const int32_t i = order[(size_t)j];
+            if (!tables_out[i]) continue;
+            const size_t words = (size_t)inst[i].g.n << inst[i].k;
+            CUDA_TRY(cudaMemcpyAsync(tables_out[i], (const int32_t *)c->b_table.ptr + pk.table_off[(size_t)j],
+                                     sizeof(int32_t) * words, cudaMemcpyDeviceToHost, st));
+        }
+        CUDA_TRY(cudaStreamSynchronize(st));
+    }
     if (stats) {
         float ms = 0;
         cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
@@ -201,6 +214,19 @@ extern "C" int emv_batch_solve(emv_ctx *c, const emv_instance *inst, int32_t cou
         stats->relax_rows = pk.rcap_used;
     }
     return EMV_OK;
+}
+
+extern "C" int emv_batch_solve(emv_ctx *c, const emv_instance *inst, int32_t count, int64_t *costs_out,
+                               emv_batch_stats *stats, void *stream)
+{
+    return batch_solve(c, inst, count, costs_out, nullptr, stats, stream);
+}
+
+extern "C" int emv_batch_solve_tables(emv_ctx *c, const emv_instance *inst, int32_t count, int64_t *costs_out,
+                                      int32_t *const *tables_out, emv_batch_stats *stats, void *stream)
+{
+    if (!tables_out) return emv_fail(EMV_ERR_BAD_INPUT, "emv_batch_solve_tables: null table list");
+    return batch_solve(c, inst, count, costs_out, tables_out, stats, stream);
 }
 
 // ---------------------------------------------------------------- packing

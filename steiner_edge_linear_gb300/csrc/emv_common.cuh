@@ -18,6 +18,14 @@ constexpr int TB_STACK = 64;
 // ctrl words of one cooperative relaxation launch (zeroed before the launch)
 enum : int { C_BAR_COUNT = 0, C_BAR_GEN = 1, C_ERR = 2, C_SLOT0 = 4, C_CNT0 = 8, C_WORDS = 12 };
 
+// Result of the device check of a CSR (k_pack_scan), zeroed before it runs.
+enum : uint32_t { SCAN_BAD_HEAD = 1, SCAN_BAD_WEIGHT = 2, SCAN_BIG_WEIGHT = 4, SCAN_BAD_ROWS = 8 };
+struct GraphScan {
+    uint32_t bad;             // SCAN_* bits
+    uint32_t maxw;            // largest arc weight
+    unsigned long long sumw;  // sum of the arc weights (both arcs of every edge)
+};
+
 // Persistent device status of one solve (zeroed at solve start).
 struct DevStat {
     uint32_t err;

@@ -22,6 +22,9 @@ int emv_dev_status_to_emv(uint32_t s)
     if (s == 0) return EMV_OK;
     if (s & (EMV_DEV_BARRIER_TIMEOUT | EMV_DEV_SWEEP_LIMIT | EMV_DEV_TB_STEPS | EMV_DEV_QUEUE_TIMEOUT))
         return emv_fail(EMV_ERR_TIMEOUT, "device loop bound reached (status 0x%x)", s);
+    if (s & EMV_DEV_BAD_VALUE) return emv_fail(EMV_ERR_BAD_INPUT, "an input value is above 2^30 (status 0x%x)", s);
+    if (s & EMV_DEV_OVERFLOW)
+        return emv_fail(EMV_ERR_OVERFLOW, "a finite value plus an arc weight reached 2^30 (status 0x%x)", s);
     return emv_fail(EMV_ERR_INTERNAL, "device status 0x%x", s);
 }
 
@@ -88,6 +91,7 @@ extern "C" int emv_create(emv_ctx **out, int32_t device)
     int st = dev_reserve(c->ctrl, sizeof(uint32_t) * C_WORDS);
     if (!st) st = dev_reserve(c->stat, sizeof(DevStat));
     if (!st) st = dev_reserve(c->lvlmax, sizeof(uint32_t) * (EMV_MAX_K + 1));
+    if (!st) st = dev_reserve(c->gscan, sizeof(GraphScan));
     if (!st) {
         if (cudaMallocHost(&c->pinned, 4096) != cudaSuccess) { cudaGetLastError(); st = emv_fail(EMV_ERR_OOM, "pinned"); }
     }
@@ -123,7 +127,7 @@ extern "C" int emv_destroy(emv_ctx *c)
     if (!c) return EMV_OK;
     cudaSetDevice(c->device);
     cudaDeviceSynchronize();
-    for (DevBuf *b : {&c->ctrl, &c->stat, &c->lvlmax, &c->shadow, &c->scratch, &c->act, &c->adj, &c->stamp, &c->terms, &c->g_row,
+    for (DevBuf *b : {&c->ctrl, &c->stat, &c->lvlmax, &c->gscan, &c->shadow, &c->scratch, &c->act, &c->adj, &c->stamp, &c->terms, &c->g_row,
                       &c->g_col, &c->g_w, &c->table, &c->tb_edges, &c->tb_out, &c->tb_work})
         dev_release(*b);
     for (KPlan *p : c->kplans) {
@@ -425,9 +429,51 @@ int launch_merge(emv_ctx *c, int32_t *table, int64_t ld, int32_t n, int32_t k, i
     return EMV_OK;
 }
 
+// Status of a device CSR check: the same statuses, bound and messages as the
+// host check emv_graph_check, whose connectivity part comes from the level-1
+// closures instead (run_dp).
+static int scan_status(const GraphScan &s, int32_t n)
+{
+    if (s.bad & SCAN_BAD_ROWS) return emv_fail(EMV_ERR_BAD_INPUT, "graph: row_ptr not from 0 to arcs, non-decreasing");
+    if (s.bad & SCAN_BAD_HEAD) return emv_fail(EMV_ERR_BAD_INPUT, "graph: arc head out of range");
+    if (s.bad & SCAN_BAD_WEIGHT) return emv_fail(EMV_ERR_BAD_INPUT, "graph: negative weight");
+    if (s.bad & SCAN_BIG_WEIGHT) return emv_fail(EMV_ERR_OVERFLOW, "graph: an arc weight reaches 2^30");
+    // every finite d[X][v] is a Steiner tree's weight: at most (n-1) * max_w
+    // and at most the weight of all edges (two arcs each)
+    const int64_t bound = std::min<int64_t>((int64_t)(n - 1) * (int64_t)s.maxw, (int64_t)(s.sumw / 2));
+    if (bound >= INF)
+        return emv_fail(EMV_ERR_OVERFLOW, "graph: table values may reach 2^30 (bound %lld)", (long long)bound);
+    return EMV_OK;
+}
+
+// Packs the arcs as int2 (c->adj) and checks the device CSR in the same
+// kernel.  With check set, waits for the check and returns its status before
+// any kernel of the DP reads the graph; the scan result stays in c->gscan.
+static int pack_and_check(emv_ctx *c, int32_t n, int64_t arcs, const int32_t *row_ptr, const int32_t *col,
+                          const int32_t *w, bool check, cudaStream_t st)
+{
+    int r = dev_reserve(c->adj, sizeof(int2) * (size_t)std::max<int64_t>(arcs, 1));
+    if (r) return r;
+    c->relax_arcs = arcs;
+    GraphScan *d_scan = (GraphScan *)c->gscan.ptr;
+    CUDA_TRY(cudaMemsetAsync(d_scan, 0, sizeof(GraphScan), st));
+    k_pack_scan<<<grid_for(std::max<int64_t>(arcs, (int64_t)n + 1), 256, 4096), 256, 0, st>>>(
+        row_ptr, n, col, w, (int2 *)c->adj.ptr, arcs, d_scan);
+    CUDA_TRY(cudaGetLastError());
+    c->launches++;
+    if (!check) return EMV_OK;
+    GraphScan *h = (GraphScan *)((char *)c->pinned + 1024);
+    CUDA_TRY(cudaMemcpyAsync(h, d_scan, sizeof(GraphScan), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return scan_status(*h, n);
+}
+
 // The DP proper on device data with packed arcs; fills the whole table.
+// With check set, a level-1 closure that left a vertex unreached (the graph
+// is not connected: the reference's table is undefined there, R:2077) makes
+// the solve EMV_ERR_DISCONNECTED; the table is then not meaningful.
 int run_dp(emv_ctx *c, int32_t n, const int32_t *row_ptr, const int2 *adj, int32_t k, const int32_t *terms_host,
-           int32_t *table, int64_t ld, cudaStream_t st, int64_t *cost_out, emv_timing *tm)
+           int32_t *table, int64_t ld, cudaStream_t st, int64_t *cost_out, emv_timing *tm, bool check)
 {
     int r = prepare_subsets(c, k, st);
     if (!r) r = reserve_relax(c, n);
@@ -527,6 +573,8 @@ int run_dp(emv_ctx *c, int32_t n, const int32_t *row_ptr, const int2 *adj, int32
     DevStat ds;
     std::memcpy(&ds, hp + 2, sizeof(ds));
     if (ds.err) return emv_dev_status_to_emv(ds.err);
+    if (check && h_max[1] >= (uint32_t)INF)
+        return emv_fail(EMV_ERR_DISCONNECTED, "graph: not connected (a vertex is unreachable from terminal 1)");
     *cost_out = (k >= 2 && hp[0] < INF) ? (int64_t)hp[0] : INT64_MAX;
     if (tm) {
         float ms = 0;
@@ -573,12 +621,9 @@ extern "C" int emv_kernel_dev(emv_ctx *c, int32_t n, int64_t arcs, const int32_t
     CUDA_TRY(cudaSetDevice(c->device));
     cudaStream_t st = (cudaStream_t)stream;
     c->launches = 0;
-    r = dev_reserve(c->adj, sizeof(int2) * (size_t)std::max<int64_t>(arcs, 1));
+    r = pack_and_check(c, n, arcs, d_row_ptr, d_col, d_w, true, st);
     if (r) return r;
-    c->relax_arcs = arcs;
-    k_pack_adj<<<grid_for(arcs, 256, 4096), 256, 0, st>>>(d_col, d_w, (int2 *)c->adj.ptr, arcs);
-    c->launches++;
-    return run_dp(c, n, d_row_ptr, (const int2 *)c->adj.ptr, k, terminals, d_table, ld, st, cost_out, nullptr);
+    return run_dp(c, n, d_row_ptr, (const int2 *)c->adj.ptr, k, terminals, d_table, ld, st, cost_out, nullptr, true);
 }
 
 // Runs the traceback kernel and reduces its edge list to a tree on the host.
@@ -659,18 +704,16 @@ int solve_on_device(emv_ctx *c, int32_t n, int64_t arcs, const int32_t *row_ptr,
                     const int32_t *w, const int32_t *terms, int32_t k, int32_t flags, emv_result *out,
                     cudaStream_t st)
 {
-    int r = dev_reserve(c->adj, sizeof(int2) * (size_t)std::max<int64_t>(arcs, 1));
+    const bool check = !(flags & EMV_SOLVE_NOCHECK);
+    int r = pack_and_check(c, n, arcs, row_ptr, col, w, check, st);
     if (r) return r;
-    c->relax_arcs = arcs;
-    k_pack_adj<<<grid_for(arcs, 256, 4096), 256, 0, st>>>(col, w, (int2 *)c->adj.ptr, arcs);
-    c->launches++;
     const int64_t ld = ((int64_t)n + 31) / 32 * 32;
     const size_t tbytes = sizeof(int32_t) * (size_t)ld << k;
     r = dev_reserve(c->table, tbytes);
     if (r) return r;
     int32_t *table = (int32_t *)c->table.ptr;
     std::memset(&out->timing, 0, sizeof(out->timing));
-    r = run_dp(c, n, row_ptr, (const int2 *)c->adj.ptr, k, terms, table, ld, st, &out->cost, &out->timing);
+    r = run_dp(c, n, row_ptr, (const int2 *)c->adj.ptr, k, terms, table, ld, st, &out->cost, &out->timing, check);
     if (r) return r;
     out->tree_count = 0;
     out->tree_weight = 0;
@@ -695,10 +738,6 @@ extern "C" int emv_solve(emv_ctx *c, const emv_graph *g, const int32_t *terminal
     if (r) return r;
     r = check_k(g->n, k, terminals);
     if (r) return r;
-    if (!(flags & EMV_SOLVE_NOCHECK)) {
-        r = emv_graph_check(g, nullptr);
-        if (r) return r;
-    }
     CUDA_TRY(cudaSetDevice(c->device));
     cudaStream_t st = (cudaStream_t)stream;
     c->launches = 0;
@@ -744,7 +783,6 @@ extern "C" int emv_sssp(emv_ctx *c, const emv_graph *g, int32_t source, int64_t 
     r = dev_reserve(c->g_row, sizeof(int32_t) * ((size_t)n + 1));
     if (!r) r = dev_reserve(c->g_col, sizeof(int32_t) * (size_t)std::max<int64_t>(arcs, 1));
     if (!r) r = dev_reserve(c->g_w, sizeof(int32_t) * (size_t)std::max<int64_t>(arcs, 1));
-    if (!r) r = dev_reserve(c->adj, sizeof(int2) * (size_t)std::max<int64_t>(arcs, 1));
     if (!r) r = dev_reserve(c->table, sizeof(int32_t) * 2 * (size_t)n);  // row 1 = {source}
     if (!r) r = dev_reserve(c->terms, sizeof(int32_t));
     if (!r) r = prepare_subsets(c, 1, st);
@@ -757,10 +795,10 @@ extern "C" int emv_sssp(emv_ctx *c, const emv_graph *g, int32_t source, int64_t 
     }
     CUDA_TRY(cudaMemcpyAsync(c->terms.ptr, &source, sizeof(int32_t), cudaMemcpyHostToDevice, st));
     CUDA_TRY(cudaMemsetAsync(c->stat.ptr, 0, sizeof(DevStat), st));
+    r = pack_and_check(c, n, arcs, (const int32_t *)c->g_row.ptr, (const int32_t *)c->g_col.ptr,
+                       (const int32_t *)c->g_w.ptr, true, st);
+    if (r) return r;
     CUDA_TRY(cudaEventRecord(c->ev[0], st));
-    c->relax_arcs = arcs;
-    k_pack_adj<<<grid_for(arcs, 256, 4096), 256, 0, st>>>((const int32_t *)c->g_col.ptr, (const int32_t *)c->g_w.ptr,
-                                                          (int2 *)c->adj.ptr, arcs);
     r = launch_relax(c, (const int32_t *)c->g_row.ptr, (const int2 *)c->adj.ptr, n, n, (int32_t *)c->table.ptr,
                      (const uint32_t *)c->kp->xs.ptr, 1, (const int32_t *)c->terms.ptr, 1, st);
     if (r) return r;

@@ -43,6 +43,45 @@ __device__ __forceinline__ bool grid_barrier(uint32_t *ctrl, int *s_ok)
     return *s_ok != 0;
 }
 
+// One thread's share of the device CSR check (grid-stride over arcs and
+// row_ptr), reduced per warp into *scan: heads in [0, n), weights in
+// [0, 2^30), row_ptr from 0 to arcs and non-decreasing, the largest weight
+// and the weight sum.  Every lane of the warp must call it.  With adj set,
+// the arcs are also packed as int2 (col, w).
+__device__ __forceinline__ void scan_csr(const int32_t *__restrict__ row_ptr, int32_t n,
+                                         const int32_t *__restrict__ col, const int32_t *__restrict__ w,
+                                         int2 *__restrict__ adj, int64_t arcs, GraphScan *__restrict__ scan)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    uint32_t bad = 0, mx = 0;
+    unsigned long long sum = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < arcs; i += stride) {
+        const int32_t c = col[i], x = w[i];
+        if (adj) adj[i] = make_int2(c, x);
+        if (c < 0 || c >= n) bad |= SCAN_BAD_HEAD;
+        if (x < 0) bad |= SCAN_BAD_WEIGHT;
+        else {
+            if (x >= INF) bad |= SCAN_BIG_WEIGHT;
+            mx = max(mx, (uint32_t)x);
+            sum += (unsigned long long)x;
+        }
+    }
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += stride) {
+        const int32_t r = row_ptr[i];
+        if (r < 0 || (int64_t)r > arcs || (i == 0 && r != 0) || (i == n && (int64_t)r != arcs) ||
+            (i < n && row_ptr[i + 1] < r))
+            bad |= SCAN_BAD_ROWS;
+    }
+    bad = __reduce_or_sync(FULL, bad);
+    mx = __reduce_max_sync(FULL, mx);
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(FULL, sum, o);
+    if ((threadIdx.x & 31) == 0) {
+        if (bad) atomicOr(&scan->bad, bad);
+        if (mx) atomicMax(&scan->maxw, mx);
+        if (sum) atomicAdd(&scan->sumw, sum);
+    }
+}
+
 // 4-byte asynchronous global -> shared copy (staging without a register round
 // trip) and the wait for all of this thread's copies.
 __device__ __forceinline__ void cp_async4(void *smem, const void *gmem)

@@ -9,6 +9,7 @@
 #include "emv_internal.h"
 
 #include <cerrno>
+#include <chrono>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -249,11 +250,10 @@ extern "C" int emv_stp_write(const emv_stp *g, const char *path)
 
 // --------------------------------------------------------------------- CSR
 
-extern "C" int emv_csr_build(int64_t n, int64_t m, const int64_t *edges, int32_t *row_ptr,
-                             int32_t *col, int32_t *w)
+// Degree count and prefix sum (R:750-792): row_ptr only.
+static int csr_pos(int64_t n, int64_t m, const int64_t *edges, int32_t *row_ptr)
 {
-    if (n <= 0 || n >= INT32_MAX || m < 0 || 2 * m >= INT32_MAX || (m > 0 && !edges) || !row_ptr ||
-        (m > 0 && (!col || !w)))
+    if (n <= 0 || n >= INT32_MAX || m < 0 || 2 * m >= INT32_MAX || (m > 0 && !edges) || !row_ptr)
         return emv_fail(EMV_ERR_BAD_INPUT, "csr: bad sizes");
     for (int64_t e = 0; e < m; e++) {
         int64_t u = edges[3 * e], v = edges[3 * e + 1], x = edges[3 * e + 2];
@@ -261,7 +261,6 @@ extern "C" int emv_csr_build(int64_t n, int64_t m, const int64_t *edges, int32_t
         if (x < 0) return emv_fail(EMV_ERR_BAD_INPUT, "csr: negative weight");
         if (x >= EMV_INF32) return emv_fail(EMV_ERR_OVERFLOW, "csr: weight %lld reaches 2^30", (long long)x);
     }
-    // Degree count and prefix sum (R:750-792), then the fill in edge order (R:794-826).
     std::vector<int64_t> deg((size_t)n + 1, 0);
     for (int64_t e = 0; e < m; e++) {
         deg[(size_t)edges[3 * e]]++;
@@ -273,6 +272,13 @@ extern "C" int emv_csr_build(int64_t n, int64_t m, const int64_t *edges, int32_t
         run += deg[(size_t)u];
     }
     row_ptr[n] = (int32_t)run;
+    return EMV_OK;
+}
+
+// The fill in edge order (R:794-826), both arcs of every edge.
+static int csr_adj(int64_t n, int64_t m, const int64_t *edges, const int32_t *row_ptr, int32_t *col, int32_t *w)
+{
+    if (m > 0 && (!col || !w)) return emv_fail(EMV_ERR_BAD_INPUT, "csr: bad sizes");
     std::vector<int64_t> fill(row_ptr, row_ptr + n);
     for (int64_t e = 0; e < m; e++) {
         int64_t u = edges[3 * e], v = edges[3 * e + 1];
@@ -281,6 +287,27 @@ extern "C" int emv_csr_build(int64_t n, int64_t m, const int64_t *edges, int32_t
         col[fill[(size_t)v]] = (int32_t)u; w[fill[(size_t)v]++] = x;
     }
     return EMV_OK;
+}
+
+extern "C" int emv_csr_build(int64_t n, int64_t m, const int64_t *edges, int32_t *row_ptr,
+                             int32_t *col, int32_t *w)
+{
+    int st = csr_pos(n, m, edges, row_ptr);
+    return st ? st : csr_adj(n, m, edges, row_ptr, col, w);
+}
+
+int emv_csr_build_timed(int64_t n, int64_t m, const int64_t *edges, int32_t *row_ptr, int32_t *col, int32_t *w,
+                        double *pos_ms, double *adj_ms)
+{
+    using clk = std::chrono::steady_clock;
+    const auto t0 = clk::now();
+    int st = csr_pos(n, m, edges, row_ptr);
+    const auto t1 = clk::now();
+    if (!st) st = csr_adj(n, m, edges, row_ptr, col, w);
+    const auto t2 = clk::now();
+    if (pos_ms) *pos_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    if (adj_ms) *adj_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();
+    return st;
 }
 
 int emv_graph_validate(const emv_graph *g)

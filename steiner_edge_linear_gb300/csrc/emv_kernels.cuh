@@ -2,12 +2,13 @@
 //
 // Table: int32 d[X * ld + v], subset-major like the reference's FV_INDEX
 // (reader/reader-el.c:691), EMV_INF32 = 2^30 for "no value".  All finite
-// values are below 2^30 (checked on the host), so a + b of two table values
+// values are below 2^30 (checked before the DP runs), so a + b of two table values
 // fits in uint32 and a value + an arc weight fits in int32.
 //
 // Kernels (reference step each one replaces):
 //   k_fill        f_v = INF                          R:2243-2259
-//   k_pack_adj    (col, w) arcs packed as int2        R:794-826 (adjacency fill)
+//   k_pack_scan   (col, w) arcs packed as int2        R:794-826 (adjacency fill)
+//                 and the device CSR checked
 //   k_merge, k_merge_smem, k_merge_stream, k_merge_stream16
 //                 subset merge of one level           R:2068-2107
 //   k_relax<VEC, U16>  multi-source closure of <= 32*VEC rows (64*VEC with
@@ -55,12 +56,16 @@ __global__ void k_fill(int32_t *__restrict__ p, int64_t count, int32_t value)
     for (; i < count; i += stride) p[i] = value;
 }
 
-__global__ void k_pack_adj(const int32_t *__restrict__ col, const int32_t *__restrict__ w,
-                           int2 *__restrict__ adj, int64_t arcs)
+// Packs the (col, w) arcs as int2 and checks the device CSR on the way (the
+// admission check of the device entry points; the reference reads only
+// well-formed STP, R:473-618): heads in [0, n), weights in [0, 2^30), row_ptr
+// from 0 to arcs and non-decreasing.  Reduces the largest weight and the
+// weight sum for the value bound.  *scan must be zero before the launch.
+__global__ void k_pack_scan(const int32_t *__restrict__ row_ptr, int32_t n, const int32_t *__restrict__ col,
+                            const int32_t *__restrict__ w, int2 *__restrict__ adj, int64_t arcs,
+                            GraphScan *__restrict__ scan)
 {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (; i < arcs; i += stride) adj[i] = make_int2(col[i], w[i]);
+    scan_csr(row_ptr, n, col, w, adj, arcs, scan);
 }
 
 // Subset merge of one level m (R:2068-2088) plus the terminal override of

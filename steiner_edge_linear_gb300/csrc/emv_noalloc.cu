@@ -15,6 +15,11 @@
 // reader/reader-el.c:1762-1880 and 2109-2130), in a variant that reads the
 // CSR's col and w arrays as given instead of a packed copy:
 //   out[r][v] = min over u of init[r][u] + dist(u, v),  r < rows <= 32.
+// Each call first checks the CSR on the device (k_noalloc_scan) and returns
+// EMV_ERR_BAD_INPUT / EMV_ERR_OVERFLOW before the closure reads it; in the
+// closure a value plus a weight saturates at EMV_INF32 instead of wrapping,
+// and a finite candidate that saturates where no smaller one exists is
+// reported as EMV_ERR_OVERFLOW.
 #include <algorithm>
 #include <mutex>
 
@@ -31,7 +36,9 @@ constexpr size_t REC_BYTES = (size_t)NOALLOC_MAX_N * NOALLOC_MAX_ROWS * sizeof(i
 constexpr size_t FLAG_BYTES = (size_t)NOALLOC_MAX_N;                                     // per flag array
 constexpr size_t CTRL_OFF = REC_BYTES + 2 * FLAG_BYTES;
 constexpr size_t STAT_OFF = CTRL_OFF + 256;
+constexpr size_t SCAN_OFF = STAT_OFF + 64;
 constexpr size_t NOALLOC_BYTES = STAT_OFF + 256;
+static_assert(SCAN_OFF + sizeof(GraphScan) <= NOALLOC_BYTES, "scan words inside the status area");
 constexpr int NOALLOC_THREADS = 512;
 constexpr int MAX_DEVICES = 64;
 
@@ -59,6 +66,22 @@ struct NoallocArgs {
     DevStat *stat;
 };
 
+// The device check of the caller's CSR, into the scratch's status area.
+__global__ void k_noalloc_scan(const int32_t *__restrict__ row_ptr, int32_t n, const int32_t *__restrict__ col,
+                               const int32_t *__restrict__ w, int64_t arcs, GraphScan *__restrict__ scan)
+{
+    scan_csr(row_ptr, n, col, w, nullptr, arcs, scan);
+}
+
+// val + wt saturated at INF (wt is in [0, INF) after the scan, val <= INF);
+// *sat is set when a finite val saturated.
+__device__ __forceinline__ int32_t sat_add(int32_t val, int32_t wt, bool *sat)
+{
+    const int32_t room = INF - wt;
+    *sat |= (val < INF) & (val >= room);
+    return min(val, room) + wt;
+}
+
 // Same phases as k_relax<1>: rows -> records, frontier sweeps, records -> rows.
 __global__ void __launch_bounds__(NOALLOC_THREADS, 2) k_closure_noalloc(NoallocArgs a)
 {
@@ -66,9 +89,14 @@ __global__ void __launch_bounds__(NOALLOC_THREADS, 2) k_closure_noalloc(NoallocA
     __shared__ int s_ok;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwb = blockDim.x >> 5;
     const int32_t n = a.n, ntiles = (n + 31) >> 5;
+    bool bad_value = false;
     for (int32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int32_t v = t * 32 + lane;
-        for (int r = warp; r < 32; r += nwb) tile[r][lane] = (r < a.rows && v < n) ? a.init[(int64_t)r * a.ld + v] : INF;
+        for (int r = warp; r < 32; r += nwb) {
+            const int32_t x = (r < a.rows && v < n) ? a.init[(int64_t)r * a.ld + v] : INF;
+            bad_value |= x > INF;
+            tile[r][lane] = min(x, INF);
+        }
         __syncthreads();
         for (int vv = warp; vv < 32; vv += nwb) {
             const int32_t v2 = t * 32 + vv;
@@ -80,6 +108,8 @@ __global__ void __launch_bounds__(NOALLOC_THREADS, 2) k_closure_noalloc(NoallocA
         a.act0[v] = 1;
         a.act1[v] = 0;
     }
+    if (__any_sync(FULL, bad_value) && lane == 0) atomicOr(&a.stat->err, (uint32_t)EMV_DEV_BAD_VALUE);
+    bool overflow = false;
     if (!grid_barrier(a.ctrl, &s_ok)) {
         if (threadIdx.x == 0) atomicOr(&a.stat->err, a.ctrl[C_ERR]);
         return;
@@ -110,6 +140,7 @@ __global__ void __launch_bounds__(NOALLOC_THREADS, 2) k_closure_noalloc(NoallocA
                 int32_t *mine = a.rec + (int64_t)vv * 32 + lane;
                 const int32_t old = __ldcg(mine);
                 int32_t acc = old;
+                bool sat = false;
                 for (int32_t e0 = beg; e0 < end; e0 += 32) {
                     int32_t cu = 0, cw = 0;
                     if (e0 + lane < end) {
@@ -126,9 +157,10 @@ __global__ void __launch_bounds__(NOALLOC_THREADS, 2) k_closure_noalloc(NoallocA
                             val[i] = (g + i < cnt) ? __ldcg(a.rec + (int64_t)u * 32 + lane) : INF;
                         }
 #pragma unroll
-                        for (int i = 0; i < 8; i++) acc = min(acc, val[i] + wt[i]);
+                        for (int i = 0; i < 8; i++) acc = min(acc, sat_add(val[i], wt[i], &sat));
                     }
                 }
+                overflow |= sat & (acc >= INF);
                 const bool dec = acc < old;
                 if (dec) __stcg(mine, acc);
                 if (__ballot_sync(FULL, dec)) {
@@ -148,6 +180,7 @@ __global__ void __launch_bounds__(NOALLOC_THREADS, 2) k_closure_noalloc(NoallocA
             break;
         }
     }
+    if (__any_sync(FULL, overflow) && lane == 0) atomicOr(&a.stat->err, (uint32_t)EMV_DEV_OVERFLOW);
     if (!converged) {
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&a.stat->err, (uint32_t)EMV_DEV_SWEEP_LIMIT);
         return;
@@ -172,6 +205,12 @@ int setup_device(int dev)
 {
     std::lock_guard<std::mutex> lk(g_setup_mu);
     if (g_scratch_ptr[dev]) return EMV_OK;
+    int coop = 0;
+    cudaError_t ec = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    if (ec != cudaSuccess || !coop) {
+        cudaGetLastError();
+        return emv_fail(EMV_ERR_CUDA, "emv_closure_noalloc: device %d does not support cooperative launches", dev);
+    }
     void *p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p) {
@@ -210,6 +249,12 @@ extern "C" int emv_closure_noalloc(int32_t n, int64_t arcs, const int32_t *d_row
     if (r) return r;
     unsigned char *base = g_scratch_ptr[dev];
     cudaStream_t st = (cudaStream_t)stream;
+    // The call waits on the stream (the check and the status reads), which a
+    // capturing stream does not allow: refuse before touching the stream.
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    CUDA_TRY(cudaStreamIsCapturing(st, &cap));
+    if (cap != cudaStreamCaptureStatusNone)
+        return emv_fail(EMV_ERR_BAD_INPUT, "emv_closure_noalloc: the stream is capturing; this call cannot be captured");
     NoallocArgs a;
     a.row_ptr = d_row_ptr;
     a.col = d_col;
@@ -224,9 +269,21 @@ extern "C" int emv_closure_noalloc(int32_t n, int64_t arcs, const int32_t *d_row
     a.act1 = base + REC_BYTES + FLAG_BYTES;
     a.ctrl = (uint32_t *)(base + CTRL_OFF);
     a.stat = (DevStat *)(base + STAT_OFF);
-    // The array keeps the last call's contents: the barrier and status words
-    // must start at zero (records and flags are rewritten by the kernel).
+    // The array keeps the last call's contents: the barrier, status and check
+    // words must start at zero (records and flags are rewritten by the kernel).
     CUDA_TRY(cudaMemsetAsync(base + CTRL_OFF, 0, NOALLOC_BYTES - CTRL_OFF, st));
+    // Check the CSR before the closure reads it (heads index the records).
+    GraphScan *d_scan = (GraphScan *)(base + SCAN_OFF), hs;
+    const int64_t scan_work = std::max<int64_t>(arcs, (int64_t)n + 1);
+    k_noalloc_scan<<<(unsigned)std::min<int64_t>(1024, (scan_work + 255) / 256), 256, 0, st>>>(d_row_ptr, n, d_col,
+                                                                                                  d_w, arcs, d_scan);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(&hs, d_scan, sizeof(hs), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    if (hs.bad & SCAN_BAD_ROWS) return emv_fail(EMV_ERR_BAD_INPUT, "emv_closure_noalloc: row_ptr not from 0 to arcs, non-decreasing");
+    if (hs.bad & SCAN_BAD_HEAD) return emv_fail(EMV_ERR_BAD_INPUT, "emv_closure_noalloc: arc head out of range");
+    if (hs.bad & SCAN_BAD_WEIGHT) return emv_fail(EMV_ERR_BAD_INPUT, "emv_closure_noalloc: negative weight");
+    if (hs.bad & SCAN_BIG_WEIGHT) return emv_fail(EMV_ERR_OVERFLOW, "emv_closure_noalloc: an arc weight reaches 2^30");
     const int vpb = NOALLOC_THREADS;  // 32 vertices per warp
     const int blocks = std::min(g_blocks[dev], std::max(1, (n + vpb - 1) / vpb));
     void *args[] = {&a};

@@ -66,6 +66,7 @@ struct emv_ctx {
     DevBuf scratch, act;           // vertex-major chunk buffer, active flags
     DevBuf stamp;                  // per vertex: last sweep in which it changed
     DevBuf adj;                    // packed (col, w) arcs
+    DevBuf gscan;                  // GraphScan of the last packed graph (device admission check)
     DevBuf terms;                  // terminals
     DevBuf g_row, g_col, g_w;      // device copy of a host CSR
     DevBuf table;                  // DP table of emv_solve

@@ -1,5 +1,6 @@
 """Batched launch and continuous-batching server: every cost equals the
-single-instance solve (and the oracle), alone and in the mix."""
+single-instance solve and the oracle, alone and in the mix; the batched
+launch's whole tables equal the reference-written golden tables."""
 import time
 
 import numpy as np
@@ -15,15 +16,45 @@ def mixed(emv):
     return [emv.Csr.from_stp(emv.StpInstance.mixed(777, i)) for i in range(80)]
 
 
-def test_batch_costs_equal_single_and_oracle(emv, orc, mixed):
+@pytest.fixture(scope="module")
+def mixed_oracle(orc, mixed):
+    """The oracle's cost of every instance of `mixed`."""
+    return [orc.emv_table(g.n, g.row_ptr, g.col, g.w, g.terminals, threads=16)[1] for g in mixed]
+
+
+def test_batch_costs_equal_single_and_oracle(emv, mixed, mixed_oracle):
     with emv.Solver(0) as s:
         costs, stats = s.batch_solve(mixed)
         single = [s.solve(g).cost for g in mixed]
-    assert list(costs) == single
-    for g, c in zip(mixed[:24], costs[:24]):
-        _, want = orc.emv_table(g.n, g.row_ptr, g.col, g.w, g.terminals, threads=8)
-        assert c == want
+    assert list(costs) == single == mixed_oracle
     assert stats["work_items"] == len(mixed) and stats["total_ms"] > 0
+
+
+def test_batch_tables_equal_reference_golden(emv, orc, golden):
+    """The 24 mixed golden cases (5 of them group instances with zero-weight
+    root arcs) in one batched launch: every instance's whole table hashes to
+    the table the reference's own emv_kernel wrote (tests/golden/golden.json),
+    and equals the oracle's cell by cell; costs equal the golden costs."""
+    from tests.golden.cases import CASES, instance_for, instance_fnv
+
+    names = sorted(n for n in CASES if n.startswith("mixed_"))
+    insts = [instance_for(CASES[n]) for n in names]
+    graphs = [emv.Csr.from_stp(i) for i in insts]
+    with emv.Solver(0) as s:
+        costs, _, tables = s.batch_solve(graphs, tables=True)
+        again, _, tables2 = s.batch_solve(graphs[::-1], tables=True)  # another launch order
+    groups = 0
+    for name, inst, g, c, t in zip(names, insts, graphs, costs, tables):
+        gold = golden["cases"][name]
+        assert instance_fnv(inst) == gold["instance_fnv"]
+        assert c == gold["cost"], name
+        assert f"{orc.fnv64(t):016x}" == gold["table_fnv"], name
+        want, _ = orc.emv_table(g.n, g.row_ptr, g.col, g.w, g.terminals, threads=8)
+        assert np.array_equal(t, want), name
+        groups += bool((inst.edges[:, 2] == 0).any())
+    assert groups >= 3
+    assert list(again[::-1]) == list(costs)
+    assert all(np.array_equal(a, b) for a, b in zip(tables, tables2[::-1]))
 
 
 def test_batch_repeat_and_autotune(emv, mixed):
@@ -59,15 +90,18 @@ def test_batch_rejects_out_of_range(emv):
         assert ei.value.status == 1
 
 
-def test_server_result_same_alone_and_in_mix(emv, mixed):
+def test_server_result_same_alone_and_in_mix(emv, orc, mixed, mixed_oracle):
     """Continuous batching: a request's cost is the same when it runs alone
     and when it shares waves with 80 others plus a large request that runs on
-    the multi-CTA path concurrently."""
+    the multi-CTA path concurrently, and every served cost equals the
+    oracle's (the large one's: equal to the plain GPU solve, whose table is
+    pinned to the reference elsewhere)."""
     probe = mixed[5]
     large = emv.Csr.from_stp(emv.StpInstance.regular(70000, 8, 1, 1000, 9, 99))
     with emv.Solver(0) as s:
         want = {i: s.solve(g).cost for i, g in enumerate(mixed)}
         want_large = s.solve(large).cost
+    assert [want[i] for i in range(len(mixed))] == mixed_oracle
     with emv.Server(0, hbm_budget_bytes=20 * 10**9, max_slots=256, large_n=65536) as srv:
         rid = srv.submit(probe)
         alone, _ = srv.wait(rid)

@@ -249,6 +249,55 @@ def test_bad_inputs_report_status(emv, solver):
     assert solver.solve(csr).cost > 0
 
 
+def test_admission_checks_on_every_entry_point(emv, solver):
+    """Weights near 2^30 are EMV_ERR_OVERFLOW, a head out of range
+    EMV_ERR_BAD_INPUT and a disconnected graph EMV_ERR_DISCONNECTED, from the
+    host entry point with its default flags and from both device entry
+    points (the device check of k_pack_scan and the level-1 connectivity
+    test), and from emv_closure_noalloc; the context solves again after each."""
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda:0")
+    stream = torch.cuda.current_stream().cuda_stream
+    base = emv.Csr.from_stp(emv.StpInstance.regular(300, 4, 1, 100, 5, 21))
+    heavy = emv.Csr(base.n, base.row_ptr, base.col, np.full_like(base.w, 1 << 28), base.terminals)
+    bad_head = emv.Csr(base.n, base.row_ptr, base.col.copy(), base.w, base.terminals)
+    bad_head.col[11] = base.n + 5
+    disc_inst = emv.StpInstance(8, np.array([[0, 1, 3], [1, 2, 4], [3, 4, 1], [4, 5, 2], [6, 7, 1], [5, 6, 9]],
+                                            np.int64), np.array([0, 2, 4], np.int64))
+    disc = emv.Csr.from_stp(disc_inst)
+    disc = emv.Csr(disc.n, disc.row_ptr, disc.col, disc.w, disc.terminals)
+    # vertices 0-2 and 3-7 are two components
+    assert disc.n == 8
+    cases = [(heavy, 8), (bad_head, 1), (disc, 7)]
+    for g, status in cases:
+        with pytest.raises(emv.EmvError) as ei:
+            solver.solve(g)
+        assert ei.value.status == status
+        row, col, w = (torch.from_numpy(a).to(dev) for a in (g.row_ptr, g.col, g.w))
+        with pytest.raises(emv.EmvError) as ei:
+            solver.solve_dev(g.n, g.arcs, row.data_ptr(), col.data_ptr(), w.data_ptr(), g.terminals, stream=stream)
+        assert ei.value.status == status
+        table = torch.empty(((1 << g.k), g.n), dtype=torch.int32, device=dev)
+        with pytest.raises(emv.EmvError) as ei:
+            solver.kernel_dev(g.n, g.arcs, row.data_ptr(), col.data_ptr(), w.data_ptr(), g.terminals,
+                              table.data_ptr(), g.n, stream)
+        assert ei.value.status == status
+        torch.cuda.synchronize()
+    # the closure entry point: a single weight of 2^30 or more, and a head out of range
+    huge = emv.Csr(base.n, base.row_ptr, base.col, base.w.copy(), base.terminals)
+    huge.w[3] = 1 << 30
+    init = torch.full((1, base.n), emv.INF32, dtype=torch.int32, device=dev)
+    init[0, 0] = 0
+    for g, status in ((huge, 8), (bad_head, 1)):
+        row, col, w = (torch.from_numpy(a).to(dev) for a in (g.row_ptr, g.col, g.w))
+        with pytest.raises(emv.EmvError) as ei:
+            emv.Solver.closure_noalloc(g.n, g.arcs, row.data_ptr(), col.data_ptr(), w.data_ptr(), init.data_ptr(), 1,
+                                       g.n, init.data_ptr(), stream)
+        assert ei.value.status == status
+    # still usable
+    assert solver.solve(base).cost == solver.solve(base, check=False).cost > 0
+
+
 def test_sweep_limit_is_a_timeout_status_and_context_survives(emv, orc):
     """A bounded device loop that runs out reports EMV_ERR_TIMEOUT through the
     status word; nothing traps and the same context solves again."""
@@ -341,10 +390,12 @@ def test_cli_dijkstra_command(emv, orc, tmp_path):
     assert int(mt.group(4)) == inst.n and int(mt.group(5)) == int(d.max())
 
 
-def test_roofline_scale_solve(emv, orc):
-    """n = 2^20, degree 10, k = 14 (the 64 GiB table): exact rows over the
-    first 6 terminals against the oracle and the closure/monotonicity
-    properties on sampled rows."""
+def test_roofline_scale_solve(emv, orc, tmp_path):
+    """n = 2^20, degree 10, k = 14 (the 64 GiB table).  d[X][v] depends only on
+    the terminals in X, so the reference's own run on the first 10 terminals
+    (ref_emv -kprefix 10: the 1024 rows X < 2^10) pins those rows of the GPU
+    table bit for bit (the oracle's first 6 terminals where the reference leg
+    is not built); closure and monotonicity on sampled rows beyond them."""
     torch = pytest.importorskip("torch")
     inst = emv.StpInstance.regular(1 << 20, 10, 1, 1024, 14, 123456789)
     csr = emv.Csr.from_stp(inst)
@@ -357,12 +408,32 @@ def test_roofline_scale_solve(emv, orc):
         cost = s.kernel_dev(n, csr.arcs, row.data_ptr(), col.data_ptr(), w.data_ptr(), csr.terminals,
                             table.data_ptr(), n, torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
-    want, _ = orc.emv_table(n, csr.row_ptr, csr.col, csr.w, csr.terminals[:6], threads=16)
-    assert np.array_equal(table[:64].cpu().numpy(), want)
+    if orc.reference_available():
+        kp = 10
+        path = str(tmp_path / "roofline.stp")
+        inst.write(path)
+        rowfnv = str(tmp_path / "rows.bin")
+        r = orc.ref_emv(path, kprefix=kp, rowfnv_out=rowfnv, threads=os.cpu_count())
+        ref_rows = np.fromfile(rowfnv, dtype="<u8")
+        assert r["k"] == kp and ref_rows.size == 1 << kp
+        h = orc.FNV_BASIS
+        got_rows = []
+        for X0 in range(0, 1 << kp, 128):
+            part = table[X0:X0 + 128].cpu().numpy()
+            h = orc.fnv64(part, h)
+            got_rows += [orc.fnv64(part[i]) for i in range(part.shape[0])]
+        bad = np.nonzero(np.array(got_rows, dtype=np.uint64) != ref_rows)[0]
+        assert bad.size == 0, f"{bad.size} rows differ from the reference, first subsets {bad[:8].tolist()}"
+        assert h == r["fnv"]
+        # the cost of the 10-terminal prefix instance is a cell of the full table
+        assert r["cost"] == int(table[(1 << (kp - 1)) - 1, int(csr.terminals[kp - 1])])
+    else:
+        want, _ = orc.emv_table(n, csr.row_ptr, csr.col, csr.w, csr.terminals[:6], threads=16)
+        assert np.array_equal(table[:64].cpu().numpy(), want)
     assert cost == int(table[(1 << (k - 1)) - 1, int(csr.terminals[k - 1])])
     src = np.repeat(np.arange(n), np.diff(csr.row_ptr))
     rng = np.random.default_rng(3)
-    for X in rng.integers(1, 1 << k, size=4):
+    for X in rng.integers(1 << 10, 1 << k, size=4):
         r = table[int(X)].cpu().numpy()
         assert (r[csr.col] <= r[src] + csr.w).all()
         for b in range(k):

@@ -3,13 +3,13 @@
 * every golden case: the C restatement's table equals the reference's
   (whole-table and per-row FNV, cost) -- the golden fixtures were written by
   the reference's own emv_kernel (tests/golden/make_golden.py);
-* the shipped test instances of the reference (testset/, read in place where
-  the reference tree exists): the restatement's cost equals each file's
+* the shipped test instances of the reference (testset/, staged unmodified
+  into the git-ignored oracle/_ref/testset/ by the oracle's recipe where the
+  reference tree exists): the restatement's cost equals each file's
   "cost" line, the check the reference itself enforces (reader-el.c:2489-2491),
   and its whole table equals the reference harness' table;
 * single-source distances against scipy's Dijkstra.
 """
-import glob
 import os
 
 import numpy as np
@@ -18,7 +18,9 @@ import pytest
 from tests.golden.cases import CASES, instance_for, instance_fnv
 from tests.helpers import table_row_fnv
 
-REF_TESTSET = "/root/reference/testset"
+import oracle
+
+REF_TESTSET = oracle.TESTSET_DIR
 
 
 @pytest.mark.parametrize("name", sorted(CASES))
@@ -35,9 +37,7 @@ def test_oracle_equals_reference_golden(name, emv, orc, golden):
 
 
 def _steinlib_files():
-    files = sorted(glob.glob(os.path.join(REF_TESTSET, "small-instances", "*", "*.stp")))
-    files += sorted(glob.glob(os.path.join(REF_TESTSET, "path", "*.stp")))
-    return files
+    return oracle.testset_files()
 
 
 @pytest.mark.skipif(not os.path.isdir(REF_TESTSET), reason="reference test instances not present")
