@@ -391,15 +391,21 @@ def test_cli_dijkstra_command(emv, orc, tmp_path):
 
 
 def test_roofline_scale_solve(emv, orc, tmp_path):
-    """n = 2^20, degree 10, k = 14 (the 64 GiB table).  d[X][v] depends only on
-    the terminals in X, so the reference's own run on the first 10 terminals
-    (ref_emv -kprefix 10: the 1024 rows X < 2^10) pins those rows of the GPU
-    table bit for bit (the oracle's first 6 terminals where the reference leg
-    is not built); closure and monotonicity on sampled rows beyond them."""
+    """n = 2^20, degree 10, k = 14 (the 64 GiB table).  With the fixture of
+    tests/golden/make_roofline_golden.py (the reference's own complete run on
+    the host cores): the whole table hashes to the reference's table and the
+    costs are equal.  Without it: d[X][v] depends only on the terminals in X,
+    so the reference's run on the first 10 terminals (ref_emv -kprefix 10:
+    the 1024 rows X < 2^10) pins those rows bit for bit (the oracle's first 6
+    terminals where the reference leg is not built).  Closure and
+    monotonicity on sampled rows either way."""
+    import json
+
     torch = pytest.importorskip("torch")
-    inst = emv.StpInstance.regular(1 << 20, 10, 1, 1024, 14, 123456789)
+    from tests.golden.make_roofline_golden import OUT as GOLDEN, SPEC, instance_fnv_fast
+
+    inst = emv.StpInstance.regular(SPEC["n"], SPEC["degree"], SPEC["wmin"], SPEC["wmax"], SPEC["k"], SPEC["seed"])
     csr = emv.Csr.from_stp(inst)
-    assert csr.check() < emv.INF32
     dev = torch.device("cuda:0")
     row, col, w = (torch.from_numpy(a).to(dev) for a in (csr.row_ptr, csr.col, csr.w))
     n, k = csr.n, csr.k
@@ -408,7 +414,25 @@ def test_roofline_scale_solve(emv, orc, tmp_path):
         cost = s.kernel_dev(n, csr.arcs, row.data_ptr(), col.data_ptr(), w.data_ptr(), csr.terminals,
                             table.data_ptr(), n, torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
-    if orc.reference_available():
+    assert cost == int(table[(1 << (k - 1)) - 1, int(csr.terminals[k - 1])])
+
+    def rows_fnv(x0, x1, h=orc.FNV_BASIS, per_row=False):
+        rows = []
+        for X0 in range(x0, x1, 256):
+            part = table[X0:min(x1, X0 + 256)].cpu().numpy()
+            h = orc.fnv64(part, h)
+            if per_row:
+                rows += [orc.fnv64(part[i]) for i in range(part.shape[0])]
+        return h, rows
+
+    if os.path.exists(GOLDEN):
+        with open(GOLDEN) as f:
+            gold = json.load(f)
+        assert instance_fnv_fast(orc, inst) == gold["instance_fnv"]
+        assert cost == gold["cost"]
+        h, _ = rows_fnv(0, 1 << k)
+        assert f"{h:016x}" == gold["table_fnv"], "whole table differs from the reference's"
+    elif orc.reference_available():
         kp = 10
         path = str(tmp_path / "roofline.stp")
         inst.write(path)
@@ -416,12 +440,7 @@ def test_roofline_scale_solve(emv, orc, tmp_path):
         r = orc.ref_emv(path, kprefix=kp, rowfnv_out=rowfnv, threads=os.cpu_count())
         ref_rows = np.fromfile(rowfnv, dtype="<u8")
         assert r["k"] == kp and ref_rows.size == 1 << kp
-        h = orc.FNV_BASIS
-        got_rows = []
-        for X0 in range(0, 1 << kp, 128):
-            part = table[X0:X0 + 128].cpu().numpy()
-            h = orc.fnv64(part, h)
-            got_rows += [orc.fnv64(part[i]) for i in range(part.shape[0])]
+        h, got_rows = rows_fnv(0, 1 << kp, per_row=True)
         bad = np.nonzero(np.array(got_rows, dtype=np.uint64) != ref_rows)[0]
         assert bad.size == 0, f"{bad.size} rows differ from the reference, first subsets {bad[:8].tolist()}"
         assert h == r["fnv"]
@@ -430,7 +449,6 @@ def test_roofline_scale_solve(emv, orc, tmp_path):
     else:
         want, _ = orc.emv_table(n, csr.row_ptr, csr.col, csr.w, csr.terminals[:6], threads=16)
         assert np.array_equal(table[:64].cpu().numpy(), want)
-    assert cost == int(table[(1 << (k - 1)) - 1, int(csr.terminals[k - 1])])
     src = np.repeat(np.arange(n), np.diff(csr.row_ptr))
     rng = np.random.default_rng(3)
     for X in rng.integers(1 << 10, 1 << k, size=4):
