@@ -12,8 +12,12 @@ namespace emv {
 
 // Grid-wide barrier for a cooperative launch.  Bounded: a block that waits
 // longer than SPIN_LIMIT iterations, or sees another block's error, records
-// the error and returns false; every block then leaves the kernel.
-__device__ __forceinline__ bool grid_barrier(uint32_t *ctrl, int *s_ok)
+// the error and returns false; every block then leaves the kernel.  after()
+// runs on thread 0 once the barrier is passed, before the block's threads
+// are released: a block reads the control words it needs there, once, into
+// shared memory, instead of every thread loading the same L2 line.
+template <typename F>
+__device__ __forceinline__ bool grid_barrier(uint32_t *ctrl, int *s_ok, F &&after)
 {
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -38,9 +42,14 @@ __device__ __forceinline__ bool grid_barrier(uint32_t *ctrl, int *s_ok)
         }
         __threadfence();
         *s_ok = (vc[C_ERR] == 0);
+        after();
     }
     __syncthreads();
     return *s_ok != 0;
+}
+__device__ __forceinline__ bool grid_barrier(uint32_t *ctrl, int *s_ok)
+{
+    return grid_barrier(ctrl, s_ok, [] {});
 }
 
 // One thread's share of the device CSR check (grid-stride over arcs and

@@ -525,7 +525,13 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
     int2 *warcs = s_arcs[threadIdx.x >> 5];
     const unsigned lt = (1u << lane) - 1;
     __shared__ unsigned s_chg;
-    if (threadIdx.x == 0) s_chg = 0;
+    // read by thread 0 after each sweep's barrier: [0] the sweep changed a
+    // record, [1] its changed count, [2] the count of the sweep before
+    __shared__ uint32_t s_ctl[3];
+    if (threadIdx.x == 0) {
+        s_chg = 0;
+        s_ctl[1] = s_ctl[2] = (uint32_t)n;
+    }
     __syncthreads();
     // Dense sweeps take every vertex (a vertex with no changed neighbour then
     // selects no arc) and so need no neighbour flags from the sweep before.
@@ -540,8 +546,8 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
     for (; s < a.max_sweeps; s++) {
         uint8_t *cur = (s & 1) ? a.act1 : a.act0;
         uint8_t *nxt = (s & 1) ? a.act0 : a.act1;
-        const uint32_t prev_chg = s == 0 ? (uint32_t)n : vctrl[C_CNT0 + (s + 3) % 4];
-        const uint32_t prev2_chg = s <= 1 ? (uint32_t)n : vctrl[C_CNT0 + (s + 2) % 4];
+        const uint32_t prev_chg = s_ctl[1];   // n before sweep 0
+        const uint32_t prev2_chg = s_ctl[2];  // n before sweeps 0 and 1
         const uint32_t pred_chg = prev_chg < prev2_chg
                                       ? (uint32_t)((uint64_t)prev_chg * prev_chg / prev2_chg)
                                       : prev_chg;
@@ -642,11 +648,16 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
             if (s_chg) atomicAdd(a.ctrl + C_CNT0 + s % 4, s_chg);
             s_chg = 0;
         }
-        if (!grid_barrier(a.ctrl, s_ok)) {
+        const bool ok = grid_barrier(a.ctrl, s_ok, [&] {
+            s_ctl[0] = vctrl[C_SLOT0 + s % 3];
+            s_ctl[2] = s_ctl[1];
+            s_ctl[1] = vctrl[C_CNT0 + s % 4];
+        });
+        if (!ok) {
             if (threadIdx.x == 0) atomicOr(&a.stat->err, a.ctrl[C_ERR]);
             return -1;
         }
-        if (vctrl[C_SLOT0 + s % 3] == 0) return s + 1;
+        if (s_ctl[0] == 0) return s + 1;
         dense = dense_next;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&a.stat->err, (uint32_t)EMV_DEV_SWEEP_LIMIT);
