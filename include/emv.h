@@ -318,13 +318,24 @@ int emv_batch_solve_tables(emv_ctx *ctx, const emv_instance *inst, int32_t count
 /* Autotuner of the batched launch (no counterpart in the reference): for
  * every instance class present in inst (n bucket <=256, <=1024, <=4096,
  * larger  x  k bucket <=6, 7-8, 9-10: EMV_BATCH_CLASSES classes), times the
- * relaxation's rows-per-chunk candidates 4, 8, 16, 32 on a sample of that
+ * relaxation's rows-per-chunk candidates 4, 8, ..., 128 on a sample of that
  * class and keeps the fastest in the context; rcap_out (may be NULL) gets
  * EMV_BATCH_CLASSES entries (0 = class not present). */
 #define EMV_BATCH_CLASSES 12
 int emv_batch_autotune(emv_ctx *ctx, const emv_instance *inst, int32_t count, int32_t *rcap_out, void *stream);
 /* Installs a previously tuned table (EMV_BATCH_CLASSES entries, 0 = default). */
 int emv_batch_set_tuning(emv_ctx *ctx, const int32_t *rcap, int32_t classes);
+/* emv_batch_autotune that also tunes the merge's tile (no counterpart in the
+ * reference): with the chosen rows-per-chunk, each class's merge vertex
+ * block of 32 * mw vertices is timed for mw = 1, 2, 4, 8 (widths whose staged
+ * rows, 2^k * 32 * mw int32, exceed the shared memory are skipped) and the
+ * fastest kept; mw_out (may be NULL) gets EMV_BATCH_CLASSES entries
+ * (0 = class not present).  The merge reads and writes the same cells
+ * whatever the width (R:2068-2107), so results do not depend on the tuning. */
+int emv_batch_autotune2(emv_ctx *ctx, const emv_instance *inst, int32_t count, int32_t *rcap_out,
+                        int32_t *mw_out, void *stream);
+/* Installs both tuned tables (EMV_BATCH_CLASSES entries each, 0 = default). */
+int emv_batch_set_tuning2(emv_ctx *ctx, const int32_t *rcap, const int32_t *mw, int32_t classes);
 
 /* -------------------------------------------------------------- serving */
 

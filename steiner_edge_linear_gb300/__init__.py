@@ -138,6 +138,8 @@ SIGNATURES = {
                                               ctypes.POINTER(_BatchStats), _P]),
     "emv_batch_autotune": (ctypes.c_int, [_P, ctypes.POINTER(_Instance), _I32, _P, _P]),
     "emv_batch_set_tuning": (ctypes.c_int, [_P, _P, _I32]),
+    "emv_batch_autotune2": (ctypes.c_int, [_P, ctypes.POINTER(_Instance), _I32, _P, _P, _P]),
+    "emv_batch_set_tuning2": (ctypes.c_int, [_P, _P, _P, _I32]),
     "emv_server_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.POINTER(_ServerOpts)]),
     "emv_server_submit": (ctypes.c_int, [_P, ctypes.POINTER(_Graph), _P, _I32, ctypes.POINTER(_I64)]),
     "emv_server_poll": (ctypes.c_int, [_P, _I64, ctypes.POINTER(_I64), ctypes.POINTER(ctypes.c_double)]),
@@ -506,6 +508,21 @@ class Solver:
     def batch_set_tuning(self, rcap) -> None:
         r = np.ascontiguousarray(rcap, dtype=np.int32)
         _check(self._lib.emv_batch_set_tuning(self._ctx, r.ctypes.data, int(r.shape[0])))
+
+    def batch_autotune_tiles(self, graphs: Sequence[Csr], stream: Optional[int] = None):
+        """Tunes the relaxation rows per chunk and the merge vertex-block width
+        per instance class (emv_batch_autotune2); returns (rcap, mw) tables."""
+        insts, _keep = self._instances(graphs)
+        rcap = np.zeros(BATCH_CLASSES, np.int32)
+        mw = np.zeros(BATCH_CLASSES, np.int32)
+        _check(self._lib.emv_batch_autotune2(self._ctx, insts, len(graphs), rcap.ctypes.data, mw.ctypes.data, stream))
+        return rcap, mw
+
+    def batch_set_tiles(self, rcap, mw) -> None:
+        """Installs both tuning tables (emv_batch_set_tuning2)."""
+        r = np.ascontiguousarray(rcap, dtype=np.int32)
+        w = np.ascontiguousarray(mw, dtype=np.int32)
+        _check(self._lib.emv_batch_set_tuning2(self._ctx, r.ctypes.data, w.ctypes.data, int(r.shape[0])))
 
     @staticmethod
     def closure_noalloc(n: int, arcs: int, row_ptr: int, col: int, w: int, init: int, rows: int, ld: int,

@@ -86,6 +86,22 @@ int32_t batch_rcap_for(const emv_ctx *c, int32_t n, int32_t k)
     return std::min(cap, pow2_floor(std::max(1, r)));
 }
 
+// Largest merge block width (in 32-vertex columns) whose staged rows fit the
+// shared memory, and no wider than the instance.
+int32_t batch_mw_max(int32_t n, int32_t k)
+{
+    int32_t mw = BATCH_MW_MAX;
+    while (mw > 1 && (((int64_t)32 * mw << k) * 4 > BATCH_SMEM_BYTES || 32 * (mw / 2) >= n)) mw /= 2;
+    return mw;
+}
+
+int32_t batch_mw_for(const emv_ctx *c, int32_t n, int32_t k)
+{
+    const int32_t cls = batch_class_of(n, k);
+    const int32_t w = (cls >= 0 && cls < BATCH_CLASSES && c->tune_mw[cls] > 0) ? c->tune_mw[cls] : 1;
+    return std::min(batch_mw_max(n, k), pow2_floor(std::max(1, w)));
+}
+
 int prepare_batch_subsets(emv_ctx *c, cudaStream_t st)
 {
     if (c->bxs_ready) return EMV_OK;
@@ -248,6 +264,7 @@ int batch_pack(emv_ctx *c, const emv_instance *inst, const std::vector<int32_t> 
         d.n = I.g.n;
         d.k = I.k;
         d.rcap = batch_rcap_for(c, I.g.n, I.k);
+        d.mw = batch_mw_for(c, I.g.n, I.k);
         d.orig = order[(size_t)j];
         d.lo = lo;
         d.hi = hi < 0 ? I.k : hi;
@@ -386,15 +403,44 @@ int batch_graph_launch(emv_ctx *c, const BatchArgs &a, int32_t count, cudaStream
 
 // --------------------------------------------------------------- autotuner
 
-// For every instance class present in `inst`, times the candidate
-// rows-per-chunk values of the relaxation on a sample of that class and keeps
-// the fastest in the context (and in *out_rcap[class] when given).
-extern "C" int emv_batch_autotune(emv_ctx *c, const emv_instance *inst, int32_t count, int32_t *out_rcap,
-                                  void *stream)
+namespace {
+
+// Device time of one batched launch over the sample `ids` with the current
+// tuning, at about four sample instances per block, as in a full batch where
+// every block solves many: the time then follows a block's throughput, not
+// the single slowest instance.  Best of three.
+int time_sample(emv_ctx *c, const emv_instance *inst, const std::vector<int32_t> &ids, cudaStream_t st, float &ms)
 {
-    if (!c || (count > 0 && !inst)) return emv_fail(EMV_ERR_BAD_INPUT, "emv_batch_autotune: bad arguments");
-    CUDA_TRY(cudaSetDevice(c->device));
-    cudaStream_t st = (cudaStream_t)stream;
+    BatchPack pk;
+    int r = batch_pack(c, inst, ids, 1, -1, pk);
+    if (!r) r = batch_upload(c, pk, st);
+    if (r) return r;
+    BatchArgs a = batch_args(c, pk);
+    const int32_t blocks = std::max<int32_t>(1, (pk.count + 3) / 4);
+    ms = 1e30f;
+    for (int rep = 0; rep < 3; rep++) {
+        CUDA_TRY(cudaEventRecord(c->ev[0], st));
+        r = launch_batch(c, a, pk.count, st, blocks);
+        if (r) return r;
+        CUDA_TRY(cudaEventRecord(c->ev[1], st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        float t = 0;
+        cudaEventElapsedTime(&t, c->ev[0], c->ev[1]);
+        ms = std::min(ms, t);
+    }
+    return EMV_OK;
+}
+
+}  // namespace
+
+// For every instance class present in `inst`, times the relaxation's
+// rows-per-chunk candidates on a sample of that class and keeps the fastest,
+// then, with it, the merge's vertex-block widths (32, 64, 128 or 256
+// vertices; candidates whose staged rows do not fit are skipped) and keeps
+// the fastest (in the context, and in out_rcap / out_mw[class] when given).
+int batch_autotune(emv_ctx *c, const emv_instance *inst, int32_t count, int32_t *out_rcap, int32_t *out_mw,
+                   cudaStream_t st)
+{
     std::vector<std::vector<int32_t>> by_class(BATCH_CLASSES);
     for (int32_t i = 0; i < count; i++) {
         if (!batch_fits(inst[i].g.n, inst[i].k)) continue;
@@ -404,39 +450,71 @@ extern "C" int emv_batch_autotune(emv_ctx *c, const emv_instance *inst, int32_t 
     for (int32_t cls = 0; cls < BATCH_CLASSES; cls++) {
         auto &ids = by_class[(size_t)cls];
         if (ids.empty()) continue;
+        int32_t nmax = 0, kmin = BATCH_KMAX;
+        for (int32_t i : ids) {
+            nmax = std::max(nmax, inst[i].g.n);
+            kmin = std::min(kmin, inst[i].k);
+        }
+        c->tune_mw[cls] = 1;
         float best_ms = 1e30f;
         int32_t best = 0;
         for (int32_t cand : {4, 8, 16, 32, 64, 128}) {
             c->tune_rcap[cls] = cand;
-            BatchPack pk;
-            int r = batch_pack(c, inst, ids, 1, -1, pk);
-            if (!r) r = batch_upload(c, pk, st);
+            float ms = 0;
+            const int r = time_sample(c, inst, ids, st, ms);
             if (r) return r;
-            BatchArgs a = batch_args(c, pk);
-            // About four sample instances per block, as in a full batch where
-            // every block solves many: the time then follows a block's
-            // throughput, not the single slowest instance.  Best of three.
-            const int32_t blocks = std::max<int32_t>(1, (pk.count + 3) / 4);
-            float ms = 1e30f;
-            for (int rep = 0; rep < 3; rep++) {
-                CUDA_TRY(cudaEventRecord(c->ev[0], st));
-                r = launch_batch(c, a, pk.count, st, blocks);
-                if (r) return r;
-                CUDA_TRY(cudaEventRecord(c->ev[1], st));
-                CUDA_TRY(cudaStreamSynchronize(st));
-                float t = 0;
-                cudaEventElapsedTime(&t, c->ev[0], c->ev[1]);
-                ms = std::min(ms, t);
-            }
             if (ms < best_ms) {
                 best_ms = ms;
                 best = cand;
             }
         }
         c->tune_rcap[cls] = best;
+        int32_t best_mw = 1;
+        for (int32_t mw = 2; mw <= BATCH_MW_MAX && mw <= batch_mw_max(nmax, kmin); mw *= 2) {
+            c->tune_mw[cls] = mw;
+            float ms = 0;
+            const int r = time_sample(c, inst, ids, st, ms);
+            if (r) return r;
+            if (ms < best_ms) {
+                best_ms = ms;
+                best_mw = mw;
+            }
+        }
+        c->tune_mw[cls] = best_mw;
     }
     if (out_rcap)
         for (int32_t cls = 0; cls < BATCH_CLASSES; cls++) out_rcap[cls] = c->tune_rcap[cls];
+    if (out_mw)
+        for (int32_t cls = 0; cls < BATCH_CLASSES; cls++) out_mw[cls] = c->tune_mw[cls];
+    return EMV_OK;
+}
+
+extern "C" int emv_batch_autotune(emv_ctx *c, const emv_instance *inst, int32_t count, int32_t *out_rcap,
+                                  void *stream)
+{
+    if (!c || (count > 0 && !inst)) return emv_fail(EMV_ERR_BAD_INPUT, "emv_batch_autotune: bad arguments");
+    CUDA_TRY(cudaSetDevice(c->device));
+    return batch_autotune(c, inst, count, out_rcap, nullptr, (cudaStream_t)stream);
+}
+
+extern "C" int emv_batch_autotune2(emv_ctx *c, const emv_instance *inst, int32_t count, int32_t *out_rcap,
+                                   int32_t *out_mw, void *stream)
+{
+    if (!c || (count > 0 && !inst)) return emv_fail(EMV_ERR_BAD_INPUT, "emv_batch_autotune2: bad arguments");
+    CUDA_TRY(cudaSetDevice(c->device));
+    return batch_autotune(c, inst, count, out_rcap, out_mw, (cudaStream_t)stream);
+}
+
+extern "C" int emv_batch_set_tuning2(emv_ctx *c, const int32_t *rcap, const int32_t *mw, int32_t classes)
+{
+    if (!c || !rcap || !mw || classes != BATCH_CLASSES)
+        return emv_fail(EMV_ERR_BAD_INPUT, "emv_batch_set_tuning2: bad arguments");
+    for (int32_t i = 0; i < classes; i++)
+        if (rcap[i] < 0 || mw[i] < 0) return emv_fail(EMV_ERR_BAD_INPUT, "emv_batch_set_tuning2: negative entry");
+    for (int32_t i = 0; i < classes; i++) {
+        c->tune_rcap[i] = rcap[i];
+        c->tune_mw[i] = mw[i];
+    }
     return EMV_OK;
 }
 

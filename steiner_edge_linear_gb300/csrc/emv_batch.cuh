@@ -4,9 +4,10 @@
 // CTA barriers only, so no grid-wide synchronisation is needed and thousands
 // of independent instances of uneven n and k share one persistent launch.
 // Per level m of an instance (reader/reader-el.c:2033-2131):
-//   merge  -- vertex blocks of 32: every row of size < m is staged in shared
-//             memory as S[Y][32], a quarter-warp computes one subset X at a
-//             time with 4 vertices per lane (R:2068-2107);
+//   merge  -- vertex blocks of 32 * mw (mw autotuned per class): every row of
+//             size < m is staged in shared memory as S[Y][32 * mw], a
+//             quarter-warp computes one subset X on one 32-vertex column of
+//             the block at a time with 4 vertices per lane (R:2068-2107);
 //   relax  -- chunks of R rows are loaded into shared memory vertex-major
 //             (stride R+1, or R+4 with 4 rows per lane), and in-place sweeps pull
 //             min(d[u] + w) over the CSR until a sweep changes nothing
@@ -25,39 +26,48 @@ __device__ __forceinline__ int32_t xs_start(const BatchArgs &a, int32_t k, int32
     return __ldg(a.xs_off + k * (BATCH_KMAX + 2) + m);
 }
 
-// Merge of level m for one instance; S holds 2^k * 32 int32.  The pair
-// loop runs on quarter-warps: the 8 lanes of a quarter hold 4 vertices each
-// (one 16-byte shared load per staged row and lane) and the four quarters of
-// a warp take four subsets of the level, which all have 2^(m-1) - 1 pairs.
+// Merge of level m for one instance; S holds 2^k * 32 * mw int32 (staged
+// rows of a block of 32 * mw vertices).  The pair loop runs on quarter-warps:
+// the 8 lanes of a quarter hold 4 vertices each of one 32-vertex column (one
+// 16-byte shared load per staged row and lane), and the four quarters of a
+// warp take four (subset, column) tasks of the level, whose subsets all have
+// 2^(m-1) - 1 pairs.  Wider blocks (mw > 1) give the low levels, which have
+// few subsets, enough tasks for every quarter-warp and stage less often.
 __device__ void batch_merge(const BatchArgs &a, int32_t *table, int32_t n, int32_t k, int32_t m,
-                            const int32_t *terms, int32_t *S)
+                            const int32_t *terms, int32_t *S, int32_t mw)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int ql = lane & 7, nq = nw * 4;
     const int32_t lo_b = xs_start(a, k, 1), lo_e = xs_start(a, k, m);       // rows of size 1..m-1
     const int32_t x_b = xs_start(a, k, m), x_e = xs_start(a, k, m + 1);     // rows of size m
     const uint32_t *xs = a.xs;
-    const uint4 *S4 = reinterpret_cast<const uint4 *>(S) + ql;  // staged row Y, this lane's 4 vertices: S4[Y * 8]
-    for (int32_t vb = 0; vb < n; vb += 32) {
-        const int32_t v = vb + lane;
+    const int32_t bw = 32 * mw;                                   // staged words of a row
+    const int32_t tasks = (x_e - x_b) * mw;                       // (subset, column) pairs
+    const uint4 *S4 = reinterpret_cast<const uint4 *>(S) + ql;  // row Y, column c, this lane: S4[Y * 8 * mw + c * 8]
+    for (int32_t vb = 0; vb < n; vb += bw) {
         // staging: 4-byte asynchronous copies, so a warp has all its rows in flight
         for (int32_t i = lo_b + warp; i < lo_e; i += nw) {
             const uint32_t Y = __ldg(xs + i);
-            if (v < n) cp_async4(S + Y * 32 + lane, table + (int64_t)Y * n + v);
-            else S[Y * 32 + lane] = INF;
+            for (int32_t c = 0; c < mw; c++) {
+                const int32_t v = vb + c * 32 + lane;
+                if (v < n) cp_async4(S + Y * bw + c * 32 + lane, table + (int64_t)Y * n + v);
+                else S[Y * bw + c * 32 + lane] = INF;
+            }
         }
         cp_async_wait_all();
         __syncthreads();
-        for (int32_t i0 = x_b + warp * 4; i0 < x_e; i0 += nq) {
-            const int32_t i = i0 + (lane >> 3);
-            const bool live = i < x_e;
-            const uint32_t X = __ldg(xs + (live ? i : x_b));
+        for (int32_t t0 = warp * 4; t0 < tasks; t0 += nq) {
+            const int32_t t = t0 + (lane >> 3);
+            const bool live = t < tasks;
+            const int32_t xi = live ? t / mw : 0, c = live ? t - xi * mw : 0;
+            const uint32_t X = __ldg(xs + x_b + xi);
             const uint32_t low = X & (0u - X), rest = X ^ low;
+            const uint4 *Sc = S4 + c * 8;
             uint4 acc = make_uint4((uint32_t)INF, (uint32_t)INF, (uint32_t)INF, (uint32_t)INF);
             uint32_t sub = 0;
             do {  // 2^(m-1) - 1 pairs {Y, X\Y}, Y holding X's lowest terminal
                 const uint32_t Y = low | sub;
-                const uint4 y = S4[Y * 8], z = S4[(X ^ Y) * 8];
+                const uint4 y = Sc[Y * 8 * mw], z = Sc[(X ^ Y) * 8 * mw];
                 acc.x = min(acc.x, y.x + z.x);
                 acc.y = min(acc.y, y.y + z.y);
                 acc.z = min(acc.z, y.z + z.z);
@@ -65,12 +75,12 @@ __device__ void batch_merge(const BatchArgs &a, int32_t *table, int32_t n, int32
                 sub = (sub - rest) & rest;
             } while (sub != rest);
             if (!live) continue;
-            const int32_t v4 = vb + ql * 4;
+            const int32_t v4 = vb + c * 32 + ql * 4;
             for (uint32_t bits = X; bits; bits &= bits - 1) {  // terminal override (R:2099-2107)
-                const int t = __ffs(bits) - 1;
-                const int32_t d = terms[t] - v4;
+                const int ti = __ffs(bits) - 1;
+                const int32_t d = terms[ti] - v4;
                 if (d < 0 || d >= 4) continue;
-                const uint32_t o = (uint32_t)S[(X ^ (1u << t)) * 32 + ql * 4 + d];
+                const uint32_t o = (uint32_t)S[(X ^ (1u << ti)) * bw + c * 32 + ql * 4 + d];
                 if (d == 0) acc.x = o;
                 else if (d == 1) acc.y = o;
                 else if (d == 2) acc.z = o;
@@ -198,7 +208,7 @@ __device__ void batch_solve_one(const BatchArgs &a, const BatchInst &I, int32_t 
             for (int32_t v = threadIdx.x; v < n; v += blockDim.x) table[v] = INF;  // row 0
             ok = batch_relax(a, table, n, row_ptr, adj, terms, xs_start(a, k, 1), xs_start(a, k, 2), I.rcap, true, S);
         } else {
-            batch_merge(a, table, n, k, m, terms, S);
+            batch_merge(a, table, n, k, m, terms, S, I.mw);
             ok = batch_relax(a, table, n, row_ptr, adj, terms, xs_start(a, k, m), xs_start(a, k, m + 1), I.rcap,
                              false, S);
         }

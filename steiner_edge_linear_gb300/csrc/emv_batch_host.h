@@ -24,6 +24,8 @@ struct BatchPack {
 int32_t batch_class_of(int32_t n, int32_t k);
 int32_t batch_rcap_max(int32_t n);
 int32_t batch_rcap_for(const emv_ctx *c, int32_t n, int32_t k);
+int32_t batch_mw_max(int32_t n, int32_t k);
+int32_t batch_mw_for(const emv_ctx *c, int32_t n, int32_t k);
 bool batch_fits(int32_t n, int32_t k);
 double batch_work(int32_t n, int32_t k, int64_t arcs);
 int prepare_batch_subsets(emv_ctx *c, cudaStream_t st);

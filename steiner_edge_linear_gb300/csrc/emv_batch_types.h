@@ -10,6 +10,7 @@ constexpr int BATCH_THREADS = 1024;
 constexpr int BATCH_KMAX = 12;
 constexpr int32_t BATCH_SMEM_BYTES = 200 * 1024;
 constexpr int32_t BATCH_RCAP_MAX = 128;  // most rows per relaxation chunk (a lane holds 4 of them)
+constexpr int32_t BATCH_MW_MAX = 8;      // widest merge vertex block: 8 columns of 32 vertices
 // Shared-memory stride of a vertex in a relaxation chunk of R rows: R + 1
 // (conflict-free single-row lanes) or, for R >= 4, R + 4 (16-byte aligned
 // 4-row lane shares).
@@ -23,6 +24,7 @@ struct BatchInst {
     int32_t n;
     int32_t k;
     int32_t rcap;            // relaxation rows per chunk (autotuned, power of two <= 32)
+    int32_t mw;              // merge vertex block of 32 * mw vertices (autotuned, 1, 2, 4 or 8)
     int32_t orig;            // slot of the cost in BatchArgs::costs
     int32_t lo;              // first level to run (1..k)
     int32_t hi;              // last level to run (lo..k)

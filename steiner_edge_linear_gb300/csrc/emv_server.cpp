@@ -208,6 +208,7 @@ void scheduler(emv_server *s)
             d.n = r->n;
             d.k = r->k;
             d.rcap = batch_rcap_for(s->ctx_small, r->n, r->k);
+            d.mw = batch_mw_for(s->ctx_small, r->n, r->k);
             d.orig = r->slot;
             d.lo = d.hi = r->next_level;
         }

@@ -88,6 +88,7 @@ struct emv_ctx {
     cudaGraphExec_t bgraph_exec = nullptr;
     char bgraph_args[160] = {};    // BatchArgs of the captured graph
     int32_t tune_rcap[BATCH_CLASSES] = {};
+    int32_t tune_mw[BATCH_CLASSES] = {};  // merge vertex-block width per class (0: default 1)
 };
 
 int prepare_subsets(emv_ctx *c, int32_t k, cudaStream_t st);

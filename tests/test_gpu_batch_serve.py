@@ -57,6 +57,33 @@ def test_batch_tables_equal_reference_golden(emv, orc, golden):
     assert all(np.array_equal(a, b) for a, b in zip(tables, tables2[::-1]))
 
 
+def test_batch_merge_tile_widths_equal_reference_golden(emv, orc, golden):
+    """The merge's vertex-block width (32 * mw vertices, tuned per class) and
+    the relaxation's rows per chunk change only the order of the work: with
+    every width forced for every class, and with the tuned tables, every
+    mixed golden instance's whole table still hashes to the reference's."""
+    from tests.golden.cases import CASES, instance_for
+
+    names = sorted(n for n in CASES if n.startswith("mixed_"))
+    graphs = [emv.Csr.from_stp(instance_for(CASES[n])) for n in names]
+    classes = emv.BATCH_CLASSES
+    with emv.Solver(0) as s:
+        for mw, rcap in ((1, 32), (2, 8), (4, 128), (8, 4)):
+            s.batch_set_tiles([rcap] * classes, [mw] * classes)
+            costs, _, tables = s.batch_solve(graphs, tables=True)
+            for name, c, t in zip(names, costs, tables):
+                gold = golden["cases"][name]
+                assert c == gold["cost"], (name, mw)
+                assert f"{orc.fnv64(t):016x}" == gold["table_fnv"], (name, mw)
+        rcap_t, mw_t = s.batch_autotune_tiles(graphs)
+        costs, _, tables = s.batch_solve(graphs, tables=True)
+    assert set(int(x) for x in rcap_t) <= {0, 4, 8, 16, 32, 64, 128} and rcap_t.max() > 0
+    assert set(int(x) for x in mw_t) <= {0, 1, 2, 4, 8} and mw_t.max() > 0
+    assert all((r > 0) == (w > 0) for r, w in zip(rcap_t, mw_t))
+    for name, c, t in zip(names, costs, tables):
+        assert f"{orc.fnv64(t):016x}" == golden["cases"][name]["table_fnv"], name
+
+
 def test_batch_repeat_and_autotune(emv, mixed):
     with emv.Solver(0) as s:
         a, _ = s.batch_solve(mixed)
