@@ -340,8 +340,18 @@ extern "C" int emv_server_create(emv_server **out, const emv_server_opts *opts)
         return st;
     }
     s->cap_slots = opts->max_slots;
-    if (cudaStreamCreateWithFlags(&s->st_small, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&s->st_large, cudaStreamNonBlocking) != cudaSuccess ||
+    // The large requests bound the stream's throughput (each needs the whole
+    // GPU for tens of milliseconds), so their stream gets the highest
+    // priority: when a wave and a large solve both have blocks waiting for
+    // SMs, the large solve's go first and its cooperative grids are not held
+    // back behind a wave.
+    int prio_least = 0, prio_greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest) != cudaSuccess) {
+        cudaGetLastError();
+        prio_least = prio_greatest = 0;
+    }
+    if (cudaStreamCreateWithPriority(&s->st_small, cudaStreamNonBlocking, prio_least) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&s->st_large, cudaStreamNonBlocking, prio_greatest) != cudaSuccess ||
         cudaMallocHost((void **)&s->h_desc, sizeof(BatchInst) * (size_t)s->cap_slots) != cudaSuccess ||
         cudaMallocHost((void **)&s->h_costs, sizeof(int64_t) * (size_t)s->cap_slots) != cudaSuccess) {
         cudaGetLastError();
