@@ -17,7 +17,10 @@ relaxations, cost read) with the CSR already resident in HBM; the working set
   batched, serve  the benchmark spec's two systems patterns measured in the same
          run: 4096 mixed instances in one persistent launch, and a Poisson
          request stream through the continuous-batching server, each against
-         plain one-instance-at-a-time GPU solves (--no-extras leaves them out)
+         plain one-instance-at-a-time GPU solves
+  roofline_scale  two timed solves of the n = 2^20, k = 14 instance (64 GiB
+         table) with their phases and the relaxation's roofline
+         (--no-extras leaves batched, serve and roofline_scale out)
 
 Other workloads alone: --workload batched, --workload serve, --workload
 roofline (n = 2^20, k = 14).  --impl reference times the reference instead
@@ -267,7 +270,7 @@ def reference_throughput(indices, base_seed: int) -> dict:
             "sample": f"{done} instances of the same distribution, one single-threaded process per core"}
 
 
-def run_single(args, dist: Dist, cfg: dict = SINGLE, cfg_name: str = SINGLE_NAME) -> dict:
+def run_single(args, dist: Dist, cfg: dict = SINGLE, cfg_name: str = SINGLE_NAME, with_e2e: bool = True) -> dict:
     import numpy as np
     import torch
 
@@ -315,7 +318,7 @@ def run_single(args, dist: Dist, cfg: dict = SINGLE, cfg_name: str = SINGLE_NAME
     pin = [torch.from_numpy(a).pin_memory() for a in (csr.row_ptr, csr.col, csr.w)]
     hcsr = E.Csr(n, pin[0].numpy(), pin[1].numpy(), pin[2].numpy(), csr.terminals)
     e2e = {}
-    for check in (True, False):
+    for check in ((True, False) if with_e2e else ()):
         for _ in range(2):
             solver.solve(hcsr, check=check, stream=sp)
         dist.barrier()
@@ -326,7 +329,7 @@ def run_single(args, dist: Dist, cfg: dict = SINGLE, cfg_name: str = SINGLE_NAME
             assert r.cost == cost
         torch.cuda.synchronize()
         e2e[check] = dist.max(time.perf_counter() - t0)
-    e2e_s = e2e[True]
+    e2e_s = e2e.get(True)
     h2d = 4 * (n + 1) + 8 * csr.arcs + 4 * k
     d2h = 4 + 16
 
@@ -349,7 +352,9 @@ def run_single(args, dist: Dist, cfg: dict = SINGLE, cfg_name: str = SINGLE_NAME
     achieved = alg / (kms / 1000.0) / 1e9
     prof = profile_traffic(f"{kname}_single") if cfg is SINGLE else None
     traffic = None
-    if prof and "dram_bytes_per_solve" in prof:
+    if prof and "dram_bytes_per_launch" in prof:
+        traffic = float(prof["dram_bytes_per_launch"])
+    elif prof and "dram_bytes_per_solve" in prof:
         traffic = prof["dram_bytes_per_solve"] / launches_k
     roofline = {"bound": "hbm", "kernel": kname, "achieved": round(achieved, 1), "peak": peak["hbm_gbs"],
                 "unit": "GB/s", "frac": round(achieved / peak["hbm_gbs"], 4),
@@ -363,10 +368,10 @@ def run_single(args, dist: Dist, cfg: dict = SINGLE, cfg_name: str = SINGLE_NAME
            "data": "synthetic (seeded generator, configuration-model random regular graph)",
            "config": single_config(cfg, cfg_name, dist.world),
            "cost": cost,
-           "e2e": {"value": round(args.steps * dist.world / e2e_s, 4), "unit": "solves/s",
-                   "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                   "call": "emv_solve, default flags (host admission checks on)",
-                   "without_host_checks": round(args.steps * dist.world / e2e[False], 4)},
+           "e2e": ({"value": round(args.steps * dist.world / e2e_s, 4), "unit": "solves/s",
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "call": "emv_solve, default flags (host admission checks on)",
+                    "without_host_checks": round(args.steps * dist.world / e2e[False], 4)} if with_e2e else None),
            "gpu_launches": launches * args.steps,
            "phases_ms": {"merge": round(merge_ms, 3), "relax_incl_level1": round(relax_ms, 3),
                          "kernel": round(kernel_ms, 3)},
@@ -404,6 +409,15 @@ def extras(args, dist) -> dict:
     out["batched"]["autotuned"] = {k: b["config"][k] for k in b["config"] if k != "workload"}
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
         out["batched"]["cpu_baseline"] = reference_throughput(range(0, 256), benchmarks.MIXED_BASE)
+    # the roofline-scale solve (n = 2^20, k = 14, 64 GiB table): two timed solves
+    short = argparse.Namespace(**vars(args))
+    short.steps, short.warmup = 2, 1
+    rf = run_single(short, dist, ROOFLINE, ROOFLINE_NAME, with_e2e=False)
+    if rf is not None:
+        out["roofline_scale"] = {k: rf[k] for k in ("value", "unit", "ms_per_step", "cost", "phases_ms",
+                                                    "relax_sweeps_per_solve", "levels_16bit", "relax_gbs_algorithmic",
+                                                    "merge_gbs_algorithmic", "roofline", "clocks")}
+        out["roofline_scale"]["workload"] = ROOFLINE_NAME
     one_rate = argparse.Namespace(**vars(args))
     one_rate.serve_rates = args.serve_rates.split(",")[-1]  # the saturating rate only
     sv = benchmarks.run_serve(one_rate, dist, clock=lambda: ClockSampler(dist.local))
