@@ -489,6 +489,90 @@ __global__ void __launch_bounds__(1024) k_merge_stream16(int32_t *__restrict__ t
     if (threadIdx.x == 0) atomicMax(level_max, s_max);
 }
 
+// A sweep that takes every vertex and pulls every arc (sweep 0, and the
+// sweeps after one that changed most vertices): the task loop of
+// relax_sweeps with the selection fixed at compile time -- no flag or stamp
+// reads, every arc of a vertex compacted -- so the compiler keeps none of the
+// other paths' state live around the gathers.  Clears this sweep's flags of
+// the warp's vertices; with flags_next, marks the neighbours of every changed
+// vertex for the next sweep.  Returns whether a record changed; counts the
+// changed vertices in *s_chg.
+template <int VEC, bool U16, int GROUP, int TASK_V>
+__device__ __forceinline__ bool relax_pass_all(const RelaxArgs &a, int32_t vbeg, int32_t vend, int32_t s,
+                                               bool flags_next, uint8_t *cur, uint8_t *nxt, int2 *warcs,
+                                               unsigned *s_chg)
+{
+    using V = typename IVec<VEC>::T;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1;
+    bool any = false;
+    for (int32_t base = vbeg; base < vend; base += TASK_V) {
+        const int32_t v = base + lane;
+        const bool mine = lane < TASK_V && v < vend;
+        unsigned act = __ballot_sync(FULL, mine);
+        if (mine) cur[v] = 0;
+        const int32_t rp0 = mine ? __ldg(a.row_ptr + v) : 0;
+        const int32_t rp1 = mine ? __ldg(a.row_ptr + v + 1) : 0;
+        int j = __ffs(act) - 1;
+        act &= act - 1;
+        int32_t beg = __shfl_sync(FULL, rp0, j), end = __shfl_sync(FULL, rp1, j);
+        int2 arc = beg + lane < end ? __ldg(a.adj + beg + lane) : make_int2(0, 0);
+        for (;;) {
+            const int32_t vv = base + j;
+            const V old = rec_ld<VEC>(a.scratch, vv, lane);
+            V acc = old;
+            for (int32_t e0 = beg;;) {
+                const int cnt = min(32, end - e0);
+                // the arcs in this warp's slots (U16: clamped weight in both halves)
+                if (lane < cnt)
+                    warcs[lane] = U16 ? make_int2(arc.x, (int32_t)(min((uint32_t)arc.y, 32768u) * 0x10001u)) : arc;
+                __syncwarp();
+                for (int i = 0; i < cnt; i += GROUP) {
+                    V val[GROUP];
+                    int32_t wt[GROUP];
+#pragma unroll
+                    for (int g = 0; g < GROUP; g++) {
+                        const bool ok = i + g < cnt;
+                        const int2 aw = warcs[(i + g) & 31];  // slots past cnt hold stale arcs: not used
+                        wt[g] = ok ? aw.y : 0;
+                        val[g] = ok ? rec_ld<VEC>(a.scratch, aw.x, lane) : vsplat<V>(U16 ? -1 : INF);
+                    }
+#pragma unroll
+                    for (int g = 0; g < GROUP; g++)
+                        acc = U16 ? vaddmin16(val[g], wt[g], acc) : vmin(acc, vadd(val[g], wt[g]));
+                }
+                __syncwarp();
+                e0 += 32;
+                if (e0 >= end) break;
+                arc = e0 + lane < end ? __ldg(a.adj + e0 + lane) : make_int2(0, 0);  // high degree: next 32 arcs
+            }
+            // the next vertex of the task before finishing this one
+            const int32_t cbeg = beg, cend = end;
+            const bool more = act != 0;
+            if (more) {
+                j = __ffs(act) - 1;
+                act &= act - 1;
+                beg = __shfl_sync(FULL, rp0, j);
+                end = __shfl_sync(FULL, rp1, j);
+                arc = beg + lane < end ? __ldg(a.adj + beg + lane) : make_int2(0, 0);
+            }
+            const bool dec = U16 ? vne(acc, old) : vlt(acc, old);
+            if (dec) rec_st<VEC>(a.scratch, vv, lane, acc);
+            if (__ballot_sync(FULL, dec)) {
+                any = true;
+                if (lane == 0) {
+                    __stcg(a.stamp + vv, s);
+                    atomicAdd(s_chg, 1u);
+                }
+                if (flags_next)
+                    for (int32_t e = cbeg + lane; e < cend; e += 32) nxt[__ldg(&a.adj[e].x)] = 1;
+            }
+            if (!more) break;
+        }
+    }
+    return any;
+}
+
 // Frontier sweeps over one chunk (phase B of k_relax).  A warp owns a
 // contiguous range of n / W vertices (W warps in the grid, so the shares
 // differ by one vertex at most) and takes them TASK_V at a time: it
@@ -559,6 +643,9 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
             vctrl[C_CNT0 + (s + 1) % 4] = 0;
         }
         bool any = false;
+        if (dense && pull_all)
+            any = relax_pass_all<VEC, U16, GROUP, TASK_V>(a, vbeg, vend, s, !dense_next, cur, nxt, warcs, &s_chg);
+        else
         for (int32_t base = vbeg; base < vend; base += TASK_V) {
             const int32_t v = base + lane;
             const bool mine = lane < TASK_V && v < vend;
