@@ -438,7 +438,7 @@ int time_sample(emv_ctx *c, const emv_instance *inst, const std::vector<int32_t>
 // then, with it, the merge's vertex-block widths (32, 64, 128 or 256
 // vertices; candidates whose staged rows do not fit are skipped) and keeps
 // the fastest (in the context, and in out_rcap / out_mw[class] when given).
-int batch_autotune(emv_ctx *c, const emv_instance *inst, int32_t count, int32_t *out_rcap, int32_t *out_mw,
+static int batch_autotune(emv_ctx *c, const emv_instance *inst, int32_t count, int32_t *out_rcap, int32_t *out_mw,
                    cudaStream_t st)
 {
     std::vector<std::vector<int32_t>> by_class(BATCH_CLASSES);
