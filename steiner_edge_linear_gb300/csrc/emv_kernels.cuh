@@ -504,7 +504,6 @@ __device__ __forceinline__ bool relax_pass_all(const RelaxArgs &a, int32_t vbeg,
 {
     using V = typename IVec<VEC>::T;
     const int lane = threadIdx.x & 31;
-    const unsigned lt = (1u << lane) - 1;
     bool any = false;
     for (int32_t base = vbeg; base < vend; base += TASK_V) {
         const int32_t v = base + lane;
@@ -573,6 +572,105 @@ __device__ __forceinline__ bool relax_pass_all(const RelaxArgs &a, int32_t vbeg,
     return any;
 }
 
+// The other sweeps: flags (or, in a dense sweep, every vertex) select the
+// vertices, stamps the arcs (unless pull_all).  A vertex is taken when its
+// flag in `flags` is set; with clear the flag is cleared first.  Returns
+// whether a record changed; counts changed vertices in *s_chg.
+template <int VEC, bool U16, int GROUP, int TASK_V>
+__device__ __forceinline__ bool relax_pass_sel(const RelaxArgs &a, int32_t vbeg, int32_t vend, int32_t s, bool dense,
+                                               bool dense_next, bool pull_all, uint8_t *flags, bool clear,
+                                               uint8_t *nxt, int2 *warcs, unsigned *s_chg)
+{
+    using V = typename IVec<VEC>::T;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1;
+    bool any = false;
+    for (int32_t base = vbeg; base < vend; base += TASK_V) {
+        const int32_t v = base + lane;
+        const bool mine = lane < TASK_V && v < vend;
+        const bool f = mine && (dense || __ldcg(flags + v) != 0);
+        unsigned act = __ballot_sync(FULL, f);
+        if (!act) continue;
+        if (f && clear) flags[v] = 0;
+        const int32_t rp0 = mine ? __ldg(a.row_ptr + v) : 0;
+        const int32_t rp1 = mine ? __ldg(a.row_ptr + v + 1) : 0;
+        // first active vertex: bounds, first 32 arcs and their selection
+        int j = __ffs(act) - 1;
+        act &= act - 1;
+        int32_t beg = __shfl_sync(FULL, rp0, j), end = __shfl_sync(FULL, rp1, j);
+        int2 arc = make_int2(0, 0);
+        bool pull = false;
+        if (beg + lane < end) {
+            arc = __ldg(a.adj + beg + lane);
+            pull = pull_all || __ldcg(a.stamp + arc.x) >= s - 1;
+        }
+        for (;;) {
+            const int32_t vv = base + j;
+            const V old = rec_ld<VEC>(a.scratch, vv, lane);
+            V acc = old;
+            for (int32_t e0 = beg;;) {
+                const unsigned sel = __ballot_sync(FULL, pull);
+                const int cnt = __popc(sel);
+                // selected arcs compacted in this warp's slots (U16: clamped weight in both halves)
+                if (pull)
+                    warcs[__popc(sel & lt)] =
+                        U16 ? make_int2(arc.x, (int32_t)(min((uint32_t)arc.y, 32768u) * 0x10001u)) : arc;
+                __syncwarp();
+                for (int i = 0; i < cnt; i += GROUP) {
+                    V val[GROUP];
+                    int32_t wt[GROUP];
+#pragma unroll
+                    for (int g = 0; g < GROUP; g++) {
+                        const bool ok = i + g < cnt;
+                        const int2 aw = warcs[(i + g) & 31];  // slots past cnt hold stale arcs: not used
+                        wt[g] = ok ? aw.y : 0;
+                        val[g] = ok ? rec_ld<VEC>(a.scratch, aw.x, lane) : vsplat<V>(U16 ? -1 : INF);
+                    }
+#pragma unroll
+                    for (int g = 0; g < GROUP; g++)
+                        acc = U16 ? vaddmin16(val[g], wt[g], acc) : vmin(acc, vadd(val[g], wt[g]));
+                }
+                __syncwarp();
+                e0 += 32;
+                if (e0 >= end) break;
+                pull = false;  // high-degree vertex: next 32 arcs
+                if (e0 + lane < end) {
+                    arc = __ldg(a.adj + e0 + lane);
+                    pull = pull_all || __ldcg(a.stamp + arc.x) >= s - 1;
+                }
+            }
+            // prefetch the next active vertex before finishing this one
+            const int32_t cbeg = beg, cend = end;
+            const bool more = act != 0;
+            if (more) {
+                j = __ffs(act) - 1;
+                act &= act - 1;
+                beg = __shfl_sync(FULL, rp0, j);
+                end = __shfl_sync(FULL, rp1, j);
+                pull = false;
+                arc = make_int2(0, 0);
+                if (beg + lane < end) {
+                    arc = __ldg(a.adj + beg + lane);
+                    pull = pull_all || __ldcg(a.stamp + arc.x) >= s - 1;
+                }
+            }
+            const bool dec = U16 ? vne(acc, old) : vlt(acc, old);
+            if (dec) rec_st<VEC>(a.scratch, vv, lane, acc);
+            if (__ballot_sync(FULL, dec)) {
+                any = true;
+                if (lane == 0) {
+                    __stcg(a.stamp + vv, s);
+                    atomicAdd(s_chg, 1u);
+                }
+                if (!dense_next)
+                    for (int32_t e = cbeg + lane; e < cend; e += 32) nxt[__ldg(&a.adj[e].x)] = 1;
+            }
+            if (!more) break;
+        }
+    }
+    return any;
+}
+
 // Frontier sweeps over one chunk (phase B of k_relax).  A warp owns a
 // contiguous range of n / W vertices (W warps in the grid, so the shares
 // differ by one vertex at most) and takes them TASK_V at a time: it
@@ -595,10 +693,8 @@ __device__ __forceinline__ bool relax_pass_all(const RelaxArgs &a, int32_t vbeg,
 template <int VEC, bool U16>
 __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
 {
-    using V = typename IVec<VEC>::T;
     constexpr int GROUP = VEC == 8 ? 2 : VEC >= 4 ? 4 : 8;  // gathers in flight per group
     constexpr int TASK_V = 8;
-    const int lane = threadIdx.x & 31;
     const int32_t n = a.n;
     const int32_t gw = (int32_t)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int32_t nwg = (int32_t)((gridDim.x * blockDim.x) >> 5);
@@ -607,7 +703,6 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
     volatile uint32_t *vctrl = a.ctrl;
     __shared__ int2 s_arcs[RELAX_THREADS / 32][32];
     int2 *warcs = s_arcs[threadIdx.x >> 5];
-    const unsigned lt = (1u << lane) - 1;
     __shared__ unsigned s_chg;
     // read by thread 0 after each sweep's barrier: [0] the sweep changed a
     // record, [1] its changed count, [2] the count of the sweep before
@@ -646,89 +741,17 @@ __device__ int32_t relax_sweeps(const RelaxArgs &a, int *s_ok)
         if (dense && pull_all)
             any = relax_pass_all<VEC, U16, GROUP, TASK_V>(a, vbeg, vend, s, !dense_next, cur, nxt, warcs, &s_chg);
         else
-        for (int32_t base = vbeg; base < vend; base += TASK_V) {
-            const int32_t v = base + lane;
-            const bool mine = lane < TASK_V && v < vend;
-            const bool f = mine && (dense || __ldcg(cur + v) != 0);
-            unsigned act = __ballot_sync(FULL, f);
-            if (!act) continue;
-            if (f) cur[v] = 0;
-            const int32_t rp0 = mine ? __ldg(a.row_ptr + v) : 0;
-            const int32_t rp1 = mine ? __ldg(a.row_ptr + v + 1) : 0;
-            // first active vertex: bounds, first 32 arcs and their selection
-            int j = __ffs(act) - 1;
-            act &= act - 1;
-            int32_t beg = __shfl_sync(FULL, rp0, j), end = __shfl_sync(FULL, rp1, j);
-            int2 arc = make_int2(0, 0);
-            bool pull = false;
-            if (beg + lane < end) {
-                arc = __ldg(a.adj + beg + lane);
-                pull = pull_all || __ldcg(a.stamp + arc.x) >= s - 1;
-            }
-            for (;;) {
-                const int32_t vv = base + j;
-                const V old = rec_ld<VEC>(a.scratch, vv, lane);
-                V acc = old;
-                for (int32_t e0 = beg;;) {
-                    const unsigned sel = __ballot_sync(FULL, pull);
-                    const int cnt = __popc(sel);
-                    // selected arcs compacted in this warp's slots (U16: clamped weight in both halves)
-                    if (pull)
-                        warcs[__popc(sel & lt)] =
-                            U16 ? make_int2(arc.x, (int32_t)(min((uint32_t)arc.y, 32768u) * 0x10001u)) : arc;
-                    __syncwarp();
-                    for (int i = 0; i < cnt; i += GROUP) {
-                        V val[GROUP];
-                        int32_t wt[GROUP];
-#pragma unroll
-                        for (int g = 0; g < GROUP; g++) {
-                            const bool ok = i + g < cnt;
-                            const int2 aw = warcs[(i + g) & 31];  // slots past cnt hold stale arcs: not used
-                            wt[g] = ok ? aw.y : 0;
-                            val[g] = ok ? rec_ld<VEC>(a.scratch, aw.x, lane) : vsplat<V>(U16 ? -1 : INF);
-                        }
-#pragma unroll
-                        for (int g = 0; g < GROUP; g++)
-                            acc = U16 ? vaddmin16(val[g], wt[g], acc) : vmin(acc, vadd(val[g], wt[g]));
-                    }
-                    __syncwarp();
-                    e0 += 32;
-                    if (e0 >= end) break;
-                    pull = false;  // high-degree vertex: next 32 arcs
-                    if (e0 + lane < end) {
-                        arc = __ldg(a.adj + e0 + lane);
-                        pull = pull_all || __ldcg(a.stamp + arc.x) >= s - 1;
-                    }
-                }
-                // prefetch the next active vertex before finishing this one
-                const int32_t cbeg = beg, cend = end;
-                const bool more = act != 0;
-                if (more) {
-                    j = __ffs(act) - 1;
-                    act &= act - 1;
-                    beg = __shfl_sync(FULL, rp0, j);
-                    end = __shfl_sync(FULL, rp1, j);
-                    pull = false;
-                    arc = make_int2(0, 0);
-                    if (beg + lane < end) {
-                        arc = __ldg(a.adj + beg + lane);
-                        pull = pull_all || __ldcg(a.stamp + arc.x) >= s - 1;
-                    }
-                }
-                const bool dec = U16 ? vne(acc, old) : vlt(acc, old);
-                if (dec) rec_st<VEC>(a.scratch, vv, lane, acc);
-                if (__ballot_sync(FULL, dec)) {
-                    any = true;
-                    if (lane == 0) {
-                        __stcg(a.stamp + vv, s);
-                        atomicAdd(&s_chg, 1u);
-                    }
-                    if (!dense_next)
-                        for (int32_t e = cbeg + lane; e < cend; e += 32) nxt[__ldg(&a.adj[e].x)] = 1;
-                }
-                if (!more) break;
-            }
-        }
+            any = relax_pass_sel<VEC, U16, GROUP, TASK_V>(a, vbeg, vend, s, dense, dense_next, pull_all, cur, true,
+                                                          nxt, warcs, &s_chg);
+        // A sparse sweep whose successor is sparse also takes, once, the vertices
+        // already marked for the next sweep (marked by changes earlier in this
+        // sweep), so a change travels two arcs per sweep in the frontier's tail.
+        // Their marks stay: the next sweep takes them again, after the barrier
+        // has made every change of this sweep visible, so a change this early
+        // pass missed is still pulled there.
+        if (!dense && !dense_next)
+            any |= relax_pass_sel<VEC, U16, GROUP, TASK_V>(a, vbeg, vend, s, false, dense_next, pull_all, nxt, false,
+                                                           nxt, warcs, &s_chg);
         any = __syncthreads_or(any);
         if (threadIdx.x == 0) {
             if (any) vctrl[C_SLOT0 + s % 3] = 1;
