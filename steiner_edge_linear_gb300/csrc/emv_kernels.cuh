@@ -681,8 +681,9 @@ __device__ __forceinline__ bool relax_pass_sel(const RelaxArgs &a, int32_t vbeg,
 // that change marked this vertex active).  The selected arcs of a window are
 // compacted into the warp's shared-memory slots, so the gather loop reads one
 // (head, weight) pair per arc instead of searching the selection mask.  The
-// arcs and stamps of the next active vertex are loaded while the current
-// one's gathers are in flight.  Only the owner writes a record and values
+// arcs and stamps of the next active vertex are requested before the current
+// one's record is stored.  Sweeps that take every vertex and pull every arc
+// run relax_pass_all, the others relax_pass_sel.  Only the owner writes a record and values
 // only decrease, so no atomics are needed.  Returns the number of sweeps, or
 // -1 after an error (recorded).
 //
