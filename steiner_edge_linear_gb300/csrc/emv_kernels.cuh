@@ -683,9 +683,9 @@ __device__ __forceinline__ bool relax_pass_sel(const RelaxArgs &a, int32_t vbeg,
 // (head, weight) pair per arc instead of searching the selection mask.  The
 // arcs and stamps of the next active vertex are requested before the current
 // one's record is stored.  Sweeps that take every vertex and pull every arc
-// run relax_pass_all, the others relax_pass_sel.  Only the owner writes a record and values
-// only decrease, so no atomics are needed.  Returns the number of sweeps, or
-// -1 after an error (recorded).
+// run relax_pass_all, the others relax_pass_sel.  Only the owner writes a
+// record and values only decrease, so no atomics are needed.  Returns the
+// number of sweeps, or -1 after an error (recorded).
 //
 // U16: 16-bit records, two rows per int32 word (64*VEC rows a record).  The
 // host takes them only when every value of the chunk's rows is at most
