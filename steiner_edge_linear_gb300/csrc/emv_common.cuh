@@ -15,8 +15,13 @@ constexpr int CHUNK_ROWS = 256;          // most int32 rows per relaxation chunk
 constexpr uint32_t SPIN_LIMIT = 1u << 22;  // grid-barrier spin iterations (~1 s with nanosleep)
 constexpr int TB_STACK = 64;
 
-// ctrl words of one cooperative relaxation launch (zeroed before the launch)
-enum : int { C_BAR_COUNT = 0, C_BAR_GEN = 1, C_ERR = 2, C_SLOT0 = 4, C_CNT0 = 8, C_WORDS = 12 };
+// ctrl words of one cooperative relaxation launch (zeroed before the launch),
+// each kind on its own 128-byte line: the barrier's arrival count, the
+// generation every block polls, the error word, the sweeps' changed flags
+// and their changed counts.  On one shared line the polls, arrivals and
+// per-sweep atomics queue behind each other at one L2 slice (a pull-all
+// sweep at n = 10^5 took 75 us instead of 58 us).
+enum : int { C_BAR_COUNT = 0, C_BAR_GEN = 32, C_ERR = 64, C_SLOT0 = 96, C_CNT0 = 128, C_WORDS = 160 };
 
 // Result of the device check of a CSR (k_pack_scan), zeroed before it runs.
 enum : uint32_t { SCAN_BAD_HEAD = 1, SCAN_BAD_WEIGHT = 2, SCAN_BIG_WEIGHT = 4, SCAN_BAD_ROWS = 8 };

@@ -32,8 +32,9 @@ __device__ __forceinline__ bool grid_barrier(uint32_t *ctrl, int *s_ok, F &&afte
         } else {
             uint32_t spins = 0;
             while (vc[C_BAR_GEN] == gen) {
-                if (vc[C_ERR] != 0) break;
-                if (++spins > SPIN_LIMIT) {
+                // another block's error is seen within 64 polls
+                if ((++spins & 63) == 0 && vc[C_ERR] != 0) break;
+                if (spins > SPIN_LIMIT) {
                     atomicOr(ctrl + C_ERR, (uint32_t)EMV_DEV_BARRIER_TIMEOUT);
                     break;
                 }

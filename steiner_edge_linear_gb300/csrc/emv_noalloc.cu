@@ -35,7 +35,8 @@ constexpr int32_t NOALLOC_MAX_ROWS = 32;       // rows per call (one per lane)
 constexpr size_t REC_BYTES = (size_t)NOALLOC_MAX_N * NOALLOC_MAX_ROWS * sizeof(int32_t);  // 16 MiB
 constexpr size_t FLAG_BYTES = (size_t)NOALLOC_MAX_N;                                     // per flag array
 constexpr size_t CTRL_OFF = REC_BYTES + 2 * FLAG_BYTES;
-constexpr size_t STAT_OFF = CTRL_OFF + 256;
+constexpr size_t STAT_OFF = CTRL_OFF + (sizeof(uint32_t) * C_WORDS + 255) / 256 * 256;
+static_assert(CTRL_OFF % 128 == 0, "control words on their own lines");
 constexpr size_t SCAN_OFF = STAT_OFF + 64;
 constexpr size_t NOALLOC_BYTES = STAT_OFF + 256;
 static_assert(SCAN_OFF + sizeof(GraphScan) <= NOALLOC_BYTES, "scan words inside the status area");
