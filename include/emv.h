@@ -346,6 +346,10 @@ typedef struct emv_server_opts {
     int64_t hbm_budget_bytes;  /* admission bound on sum of 2^k*n*4       */
     int32_t max_slots;         /* requests resident at once                */
     int32_t large_n;           /* n at or above which a request runs alone */
+    int32_t wave_sms;          /* SMs kept for the small requests' waves
+                                  while a large request runs: 0 = a sixth
+                                  of the SMs, < 0 = none (waves and large
+                                  solves then take turns on the whole GPU) */
 } emv_server_opts;
 
 typedef struct emv_server_stats {

@@ -94,7 +94,7 @@ class _BatchStats(ctypes.Structure):
 
 class _ServerOpts(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_int64), ("max_slots", ctypes.c_int32),
-                ("large_n", ctypes.c_int32)]
+                ("large_n", ctypes.c_int32), ("wave_sms", ctypes.c_int32)]
 
 
 class _ServerStats(ctypes.Structure):
@@ -552,10 +552,12 @@ class Server:
     """Continuous-batching request loop on one GPU (emv_server_*)."""
 
     def __init__(self, device: int = 0, hbm_budget_bytes: int = 150 * 10**9, max_slots: int = 4096,
-                 large_n: int = 65536):
+                 large_n: int = 65536, wave_sms: int = 0):
+        """wave_sms: SMs kept for the small requests while a large one runs
+        (0: a sixth of the SMs; negative: no split)."""
         self._lib = load_library()
         self._srv = ctypes.c_void_p()
-        opts = _ServerOpts(device, hbm_budget_bytes, max_slots, large_n)
+        opts = _ServerOpts(device, hbm_budget_bytes, max_slots, large_n, wave_sms)
         _check(self._lib.emv_server_create(ctypes.byref(self._srv), ctypes.byref(opts)))
         self._keep: dict[int, Csr] = {}
 

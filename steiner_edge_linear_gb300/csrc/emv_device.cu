@@ -198,7 +198,9 @@ int launch_relax(emv_ctx *c, const int32_t *row_ptr, const int2 *adj, int32_t n,
     const void *fn = relax_fns[vi];
     // A warp per 8 vertices is enough; small graphs use fewer blocks (cheaper barriers).
     const int vpb = 8 * (RELAX_THREADS / 32);
-    const int blocks = std::min(c->relax_blocks_max[vi], std::max(1, (n + vpb - 1) / vpb));
+    int bmax = c->relax_blocks_max[vi];
+    if (c->relax_sm_cap > 0 && c->relax_sm_cap < c->sms) bmax = std::max(1, bmax / c->sms * c->relax_sm_cap);
+    const int blocks = std::min(bmax, std::max(1, (n + vpb - 1) / vpb));
     CUDA_TRY(cudaMemsetAsync(a.ctrl, 0, sizeof(uint32_t) * C_WORDS, st));
     void *args[] = {&a};
     CUDA_TRY(cudaLaunchCooperativeKernel(fn, dim3(blocks), dim3(RELAX_THREADS), args, 0, st));

@@ -10,8 +10,14 @@
 // across levels (stream-ordered allocations).  Requests too large for one
 // CTA (n above large_n, or k above the batched range) go to a second worker
 // that runs the multi-CTA solver on its own stream, concurrently with the
-// waves.  Every call is thread-safe.
+// waves.  A wave block takes a whole SM, and a relaxation grid must be
+// resident at once, so while a large request runs with small ones resident
+// the two split the SMs: the large solve's relaxation grids are sized for
+// all but wave_sms SMs, and the waves launch at most wave_sms blocks (one per
+// SM).  Neither then waits for the other's blocks to drain.  Every call is
+// thread-safe.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -85,6 +91,8 @@ struct emv_server {
     BatchInst *h_desc = nullptr;
     int64_t *h_costs = nullptr;
     int32_t cap_slots = 0;
+    int32_t wave_sms = 0;                  // SMs the waves keep while a large request runs (0: no split)
+    std::atomic<bool> large_sharing{false};  // a large solve runs on the other SMs
 };
 
 namespace {
@@ -226,7 +234,9 @@ void scheduler(emv_server *s)
         if (cudaMemcpyAsync(s->d_desc.ptr, s->h_desc, sizeof(BatchInst) * wave.size(), cudaMemcpyHostToDevice,
                             s->st_small) != cudaSuccess)
             st = emv_fail(EMV_ERR_CUDA, "server: descriptor upload");
-        if (!st) st = launch_batch(s->ctx_small, a, a.count, s->st_small);
+        // beside a large solve the wave stays on its share of the SMs
+        const int32_t wave_blocks = s->large_sharing.load() ? s->wave_sms : 0;
+        if (!st) st = launch_batch(s->ctx_small, a, a.count, s->st_small, wave_blocks);
         if (!st && cudaMemcpyAsync(s->h_costs, s->d_costs.ptr, sizeof(int64_t) * (size_t)s->cap_slots,
                                    cudaMemcpyDeviceToHost, s->st_small) != cudaSuccess)
             st = emv_fail(EMV_ERR_CUDA, "server: cost read");
@@ -293,11 +303,16 @@ void large_loop(emv_server *s)
             s->resident_count++;
             s->stats.peak_resident = std::max<int64_t>(s->stats.peak_resident, s->resident_count);
             s->stats.peak_bytes = std::max<int64_t>(s->stats.peak_bytes, s->resident_bytes);
+            // split the SMs only when there are small requests to run beside it
+            const bool share = s->wave_sms > 0 && (!s->resident.empty() || !s->queue_small.empty());
+            s->ctx_large->relax_sm_cap = share ? s->ctx_large->sms - s->wave_sms : 0;
+            s->large_sharing = share;
         }
         emv_graph g{r->n, r->arcs, r->row.data(), r->col.data(), r->w.data()};
         emv_result res;
         std::memset(&res, 0, sizeof(res));
         int st = emv_solve(s->ctx_large, &g, r->terms.data(), r->k, EMV_SOLVE_NOCHECK, &res, s->st_large);
+        s->large_sharing = false;
         std::lock_guard<std::mutex> lk(s->mu);
         s->resident_bytes -= r->bytes;
         s->resident_count--;
@@ -340,6 +355,11 @@ extern "C" int emv_server_create(emv_server **out, const emv_server_opts *opts)
         return st;
     }
     s->cap_slots = opts->max_slots;
+    {
+        const int sms = s->ctx_large->sms;
+        const int want = opts->wave_sms == 0 ? std::max(1, sms / 6) : opts->wave_sms;
+        s->wave_sms = (want > 0 && want < sms) ? want : 0;
+    }
     // The large requests bound the stream's throughput (each needs the whole
     // GPU for tens of milliseconds), so their stream gets the highest
     // priority: when a wave and a large solve both have blocks waiting for

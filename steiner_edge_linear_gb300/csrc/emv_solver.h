@@ -54,6 +54,7 @@ struct emv_ctx {
     int device = 0;
     int sms = 0;
     int relax_blocks_max[RELAX_VARIANTS] = {};  // cooperative grid of each relaxation kernel
+    int relax_sm_cap = 0;          // > 0: relaxation grids sized for this many SMs (the server's large solves)
     int64_t l2_bytes = 0;
     int64_t sweep_limit = 0;       // relaxation sweeps per chunk, 0 = n + 1
     int32_t value_bits = 0;        // 0: 16-bit merge staging / relaxation records where bounded, 32: never
