@@ -117,26 +117,32 @@ def test_batch_rejects_out_of_range(emv):
         assert ei.value.status == 1
 
 
-def test_server_result_same_alone_and_in_mix(emv, orc, mixed, mixed_oracle):
+@pytest.mark.parametrize("wave_sms", [0, -1, 3])
+def test_server_result_same_alone_and_in_mix(emv, orc, mixed, mixed_oracle, wave_sms):
     """Continuous batching: a request's cost is the same when it runs alone
     and when it shares waves with 80 others plus a large request that runs on
     the multi-CTA path concurrently, and every served cost equals the
     oracle's (the large one's: equal to the plain GPU solve, whose table is
-    pinned to the reference elsewhere)."""
+    pinned to the reference elsewhere).  wave_sms: the default split of the
+    SMs beside a large solve, none (waves and the large solve take turns),
+    and a narrow one (waves on 3 SMs, the large solve's relaxation grids on
+    the rest)."""
     probe = mixed[5]
     large = emv.Csr.from_stp(emv.StpInstance.regular(70000, 8, 1, 1000, 9, 99))
     with emv.Solver(0) as s:
         want = {i: s.solve(g).cost for i, g in enumerate(mixed)}
         want_large = s.solve(large).cost
     assert [want[i] for i in range(len(mixed))] == mixed_oracle
-    with emv.Server(0, hbm_budget_bytes=20 * 10**9, max_slots=256, large_n=65536) as srv:
+    with emv.Server(0, hbm_budget_bytes=20 * 10**9, max_slots=256, large_n=65536, wave_sms=wave_sms) as srv:
         rid = srv.submit(probe)
         alone, _ = srv.wait(rid)
         assert alone == want[5]
         ids = {}
-        lid = srv.submit(large)
+        lid = None
         for i, g in enumerate(mixed):
             ids[srv.submit(g)] = i
+            if i == 20:
+                lid = srv.submit(large)  # starts with small requests resident: the SMs are split
             if i % 10 == 0:
                 time.sleep(0.002)  # arrivals while earlier requests are on the GPU
         for r, i in ids.items():
