@@ -14,7 +14,7 @@ relaxations, cost read) with the CSR already resident in HBM; the working set
   roofline  the dominant kernel against the measured HBM copy bandwidth
   cpu_baseline  the reference's own emv_kernel (oracle/_ref) on the box's
          host cores, on a bounded sample of the same workload
-  batched, serve  the benchmark spec's two systems patterns measured in the same
+  batched, serve  the batching and serving paths measured in the same
          run: 4096 mixed instances in one persistent launch, and a Poisson
          request stream through the continuous-batching server, each against
          plain one-instance-at-a-time GPU solves
@@ -396,7 +396,7 @@ def run_single(args, dist: Dist, cfg: dict = SINGLE, cfg_name: str = SINGLE_NAME
 
 def extras(args, dist) -> dict:
     """The batched and serving workloads of the default line, each with its
-    own clocks: the benchmark spec's batched/served solves/s against plain
+    own clocks: batched and served solves/s against plain
     one-instance-at-a-time GPU solves (config: 4096 mixed instances; a
     Poisson stream at one saturating arrival rate)."""
     from steiner_edge_linear_gb300 import benchmarks
