@@ -1,7 +1,7 @@
-"""The oracle: CPU checkers of the GPU EMV solver.
+"""The oracle: CPU restatements that the GPU EMV solver is compared with.
 
 TEST INFRASTRUCTURE ONLY.  tests/, the smoke check of __graft_entry__ and the
-CPU-baseline leg of bench.py use this package as the checker; the solver's
+CPU-baseline leg of bench.py use this package as the oracle; the solver's
 product code never imports it.
 
 Two legs:

@@ -3,8 +3,8 @@
  * program computed by the reference solver, written from scratch in plain C.
  *
  * TEST INFRASTRUCTURE ONLY.  This is the oracle: the parity tests, the smoke
- * check and the CPU-baseline leg of bench.py call it as the checker of the
- * GPU solver.  No product code path links, loads or calls it.
+ * check and the CPU-baseline leg of bench.py compare the GPU solver with
+ * it.  No product code path links, loads or calls it.
  *
  * What it restates (file:line in the reference project):
  *   - dijkstra()            reader/reader-el.c:1762-1880  single/multi-source SSSP
