@@ -22,6 +22,9 @@ constexpr int TB_STACK = 64;
 // per-sweep atomics queue behind each other at one L2 slice (a pull-all
 // sweep at n = 10^5 took 75 us instead of 58 us).
 enum : int { C_BAR_COUNT = 0, C_BAR_GEN = 32, C_ERR = 64, C_SLOT0 = 96, C_CNT0 = 128, C_WORDS = 160 };
+static_assert(C_BAR_GEN - C_BAR_COUNT >= 32 && C_ERR - C_BAR_GEN >= 32 && C_SLOT0 - C_ERR >= 32 &&
+                  C_CNT0 - C_SLOT0 >= 32 && C_WORDS - C_CNT0 >= 32,
+              "each kind of control word on its own 128-byte line");
 
 // Result of the device check of a CSR (k_pack_scan), zeroed before it runs.
 enum : uint32_t { SCAN_BAD_HEAD = 1, SCAN_BAD_WEIGHT = 2, SCAN_BIG_WEIGHT = 4, SCAN_BAD_ROWS = 8 };
